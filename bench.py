@@ -1,0 +1,372 @@
+"""Benchmark of the fused sequential raytrace on one GB300 (or N replicas).
+
+Workload (default): the precision form -- the Newtonian telescope (parabolic
+primary R = -800 mm behind a 12 mm obscuration, 45 degree fold, 1024^2 sensor
+of 13.5 um pixels) with both mirrors Al-coated (substrate Fresnel from a
+seeded 3-point complex index table), 1e8 rays per GPU: field uniform in the
++-0.15 deg square, pupil uniform on the 12-50 mm annulus, wavelength uniform
+on 400-700 nm.  One step = ``rayfunction`` with sensor binning: every ray
+through the 5 surfaces (object, obscuration, primary, fold, sensor), outputs
+position, direction, intensity, OPL and mask in the sensor frame, plus the
+count and flux images.  Metric: rays*surfaces/s.
+
+``value`` times the kernel with inputs resident in HBM; ``e2e`` times the
+public ``SequentialSystem.rayfunction`` call from pinned host arrays with the
+host->device input copy and the device->host copy of every output inside the
+timed region.  ``--impl reference`` times the CPU path (the float64 NumPy
+restatement of the reference's trace, all host cores) on a bounded sample.
+
+Multi-GPU: rays are independent, so each rank traces its own 1e8 rays with
+no collective on the data path (weak scaling); value = all ranks' work over
+the slowest rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import pathlib
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "rays*surfaces/s (fused FP32 sequential raytrace, precision form)"
+UNIT = "rays*surfaces/s"
+NUM_SURFACES = 5
+
+# Algorithmic cost of one ray of this workload (counted from the device code
+# path: object, obscuration, coated primary, coated fold, sensor), see the
+# design notes.  Bytes: read 5 x 4 B inputs; write 6 x 4 B position and
+# direction, 4 B intensity, 8 B OPL, 1 B mask.
+BYTES_PER_RAY = 5 * 4 + 6 * 4 + 4 + 8 + 1
+
+
+def _cpu_worker(args):
+    """One bounded chunk of the CPU baseline (float64 NumPy restatement)."""
+    n, seed = args
+    sys.path.insert(0, str(ROOT))
+    from optika_gb300 import configs
+    from oracle import trace as O
+
+    system = configs.newtonian(coated=True)
+    g = configs.precision_grid(n, seed=seed)
+    t0 = time.perf_counter()
+    r = O.rayfunction(system, g["wavelength"], g["field_x"], g["field_y"], g["pupil_x"],
+                      g["pupil_y"])
+    O.collect(system.sensor, r)
+    return n, time.perf_counter() - t0
+
+
+def cpu_baseline(total_rays: int, cores: int) -> tuple[float, float]:
+    """Throughput (rays*surfaces/s) of the CPU path over `cores` processes."""
+    import concurrent.futures
+    import multiprocessing as mp
+
+    chunk = max(1, total_rays // cores)
+    ctx = mp.get_context("spawn")
+    with concurrent.futures.ProcessPoolExecutor(max_workers=cores, mp_context=ctx) as ex:
+        list(ex.map(_cpu_worker, [(1000, 7)] * cores))  # warm the workers
+        t0 = time.perf_counter()
+        res = list(ex.map(_cpu_worker, [(chunk, 100 + i) for i in range(cores)]))
+        wall = time.perf_counter() - t0
+    rays = sum(r[0] for r in res)
+    return rays * NUM_SURFACES / wall, wall
+
+
+class Clocks:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{index}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.f, stderr=subprocess.DEVNULL,
+            )
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks() -> tuple[dict, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def run_reference(args, rank: int, world: int) -> None:
+    if rank != 0:
+        return
+    cores = len(os.sched_getaffinity(0))
+    # each step: a bounded sample of the workload spread over all host cores
+    per_step = args.cpu_rays
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, wall = cpu_baseline(per_step, cores)
+        if i >= args.warmup:
+            vals.append((v, wall))
+    value = float(np.mean([v for v, _ in vals]))
+    wall = float(np.mean([w for _, w in vals]))
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": wall * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded numpy)",
+        "config": {"workload": "newtonian-precision (Al-coated mirrors, 400-700 nm)",
+                   "rays_per_step": per_step, "surfaces": NUM_SURFACES},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{per_step} rays per step over {cores} processes"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--rays", type=int, default=100_000_000)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-rays", type=int, default=8_000_000)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--rays-per-thread", type=int, default=0)
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    import optika_gb300 as ok
+    from optika_gb300 import _api, _lib, configs
+
+    V = ok.vectors.Cartesian2dVectorArray
+    system = configs.newtonian(coated=True)
+    n = args.rays
+    g = configs.precision_grid(n, seed=2 + 7919 * rank)
+    dev = torch.device("cuda", local)
+    host = {k: torch.from_numpy(v.astype(np.float32)).pin_memory() for k, v in g.items()}
+    inp = {k: v.to(dev) for k, v in host.items()}
+    launch = _lib.Launch()
+    launch.rays_per_thread = args.rays_per_thread
+    outputs = ("px", "py", "pz", "dx", "dy", "dz", "intensity", "unvignetted", "opl")
+    prep = _api.PreparedTrace(
+        system, wavelength=inp["wavelength"], field=V(inp["field_x"], inp["field_y"]),
+        pupil=V(inp["pupil_x"], inp["pupil_y"]), final_local=True, image=True, launch=launch,
+        outputs=outputs,
+    )
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        prep.run()
+    torch.cuda.synchronize()
+    barrier()
+
+    clocks = Clocks(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier()
+    start.record(stream)
+    for i in range(args.steps):
+        prep.counts.zero_()
+        prep.flux.zero_()
+        ev[i][0].record(stream)
+        st = prep.lib.otx_trace_grid(
+            _api.ctypes.byref(prep.lowering.sys), _api.ctypes.byref(prep.grid),
+            _api.ctypes.byref(prep.out), _api.ctypes.byref(prep.img),
+            _api.ctypes.byref(prep.launch_desc), _api.stream_handle(),
+        )
+        _lib.check(st, "otx_trace_grid")
+        ev[i][1].record(stream)
+    stop.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    total_ms = start.elapsed_time(stop)
+    kernel_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    ms_step = total_ms / args.steps
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * n * NUM_SURFACES / (ms_step * 1e-3)
+
+    # end to end: public API from pinned host arrays, every output back to host
+    h2d = sum(v.numel() * v.element_size() for v in host.values())
+    out_host = None
+    e2e_ms = []
+    for i in range(args.e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d = {k: v.to(dev, non_blocking=True) for k, v in host.items()}
+        res = system.rayfunction(
+            wavelength=d["wavelength"], field=V(d["field_x"], d["field_y"]),
+            pupil=V(d["pupil_x"], d["pupil_y"]), normalized_field=False,
+            normalized_pupil=False, image=True, launch=launch,
+        )
+        o = res.outputs
+        tensors = [o.position.x, o.position.y, o.position.z, o.direction.x, o.direction.y,
+                   o.direction.z, o.intensity, o.opl, res.image[0], res.image[1]]
+        tensors.append(o.unvignetted)
+        if out_host is None:
+            out_host = [torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for t in tensors]
+        for hst, t in zip(out_host, tensors):
+            hst.copy_(t, non_blocking=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if i > 0:
+            e2e_ms.append(dt * 1e3)
+        del res, o, tensors, d
+    d2h = sum(t.numel() * t.element_size() for t in out_host)
+    e2e_ms_step = float(np.median(e2e_ms))
+    e2e_value = world * n * NUM_SURFACES / (e2e_ms_step * 1e-3)
+
+    pk, pk_kind = peaks()
+    achieved = BYTES_PER_RAY * n / (kernel_ms * 1e-3) / 1e9
+    roofline = {
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": pk["hbm_gbs"],
+        "unit": "GB/s",
+        "frac": achieved / pk["hbm_gbs"],
+        "traffic": None,
+        "peak_kind": pk_kind,
+        "kernel": "k_trace<rpt,GRID_INFINITY,false>",
+        "kernel_ms": kernel_ms,
+        "bytes_per_ray": BYTES_PER_RAY,
+    }
+    prof = ROOT / "profiles" / "trace_precision_1e8.json"
+    if prof.exists():
+        pj = json.loads(prof.read_text())
+        if pj.get("dram_bytes_per_ray"):
+            roofline["traffic"] = pj["dram_bytes_per_ray"] * n
+        if pj.get("flops_per_ray"):
+            fl = pj["flops_per_ray"]
+            roofline["fp32_flops_per_ray"] = fl
+            roofline["fp32_tflops_achieved"] = fl * n / (kernel_ms * 1e-3) / 1e12
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores = len(os.sched_getaffinity(0))
+        v, wall = cpu_baseline(args.cpu_rays, cores)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{args.cpu_rays} rays of the same workload over {cores} processes "
+                         f"({wall:.1f} s)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic (seeded numpy)",
+            "config": {
+                "workload": "newtonian-precision (Al-coated mirrors, 400-700 nm)",
+                "rays_per_gpu": n,
+                "surfaces": NUM_SURFACES,
+                "sensor": "1024x1024 x 13.5um, uint32 counts + float flux",
+                "l2": "inputs (2 GB) and outputs larger than L2; no flush",
+            },
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_ms_step,
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

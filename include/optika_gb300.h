@@ -1,0 +1,281 @@
+/*
+ * optika_gb300 C-ABI: the drop-in boundary of the GB300 sequential raytracer.
+ *
+ * Every entry point takes plain pointers and sizes (device pointers for ray
+ * and image buffers, a host pointer for the packed system descriptor) and a
+ * cudaStream_t passed as `void*`.  Nothing here allocates device memory on
+ * the hot path; every buffer is owned by the caller.
+ *
+ * The reference (optika, pure Python) has no FFI.  Each function below
+ * replaces a Python call chain of the reference, cited beside it
+ * (file:line within the optika project).  Units are fixed: lengths in mm,
+ * vacuum wavelengths in nm, angles in radians, attenuation in 1/mm.
+ */
+#ifndef OPTIKA_GB300_H
+#define OPTIKA_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OTX_ABI_VERSION 1
+
+#define OTX_MAX_SURFACES 16
+#define OTX_MAX_POLY_TERMS 8
+#define OTX_MAX_VERTICES 64
+#define OTX_MAX_LAYERS 64
+#define OTX_MAX_STACKS 4
+
+/* ---- status codes ---------------------------------------------------- */
+typedef int32_t otx_status;
+#define OTX_OK 0
+#define OTX_ERR_INVALID 1     /* bad descriptor or argument              */
+#define OTX_ERR_UNSUPPORTED 2 /* a type tag this build does not know      */
+#define OTX_ERR_CUDA 3        /* a CUDA runtime call failed              */
+#define OTX_ERR_SIZE 4        /* a size exceeds a documented maximum      */
+#define OTX_ERR_TIMEOUT 5     /* a bounded device wait gave up            */
+
+/* ---- type tags ------------------------------------------------------- */
+#define OTX_SAG_FLAT 0     /* optika/sags/_flat.py:13              NoSag        */
+#define OTX_SAG_SPHERE 1   /* optika/sags/_spherical.py:40         SphericalSag */
+#define OTX_SAG_CONIC 2    /* optika/sags/_conic.py:16             ConicSag     */
+#define OTX_SAG_PARABOLA 3 /* optika/sags/_parabolic.py:14         ParabolicSag */
+#define OTX_SAG_TOROID 4   /* optika/sags/_toroidal.py:14          ToroidalSag  */
+
+#define OTX_MAT_VACUUM 0            /* optika/materials/_materials.py:82  */
+#define OTX_MAT_MIRROR 1            /* optika/materials/_materials.py:161 */
+#define OTX_MAT_GLASS 2             /* optika/materials/_materials.py:309 */
+#define OTX_MAT_MULTILAYER_MIRROR 3 /* optika/materials/_multilayers.py:908 */
+#define OTX_MAT_MULTILAYER_FILM 4   /* optika/materials/_multilayers.py:839 */
+
+#define OTX_APER_NONE 0
+#define OTX_APER_CIRCULAR 1    /* optika/apertures/_apertures.py:292 */
+#define OTX_APER_RECTANGULAR 2 /* optika/apertures/_apertures.py:941 */
+#define OTX_APER_ELLIPTICAL 3  /* optika/apertures/_apertures.py:640 */
+#define OTX_APER_SECTOR 4      /* optika/apertures/_apertures.py:438 */
+#define OTX_APER_POLYGON 5     /* optika/apertures/_apertures.py:739 */
+
+#define OTX_APER_FLAG_INVERTED 1
+#define OTX_APER_FLAG_ACTIVE 2
+#define OTX_APER_FLAG_DIRECTION 4 /* dimensionless aperture: tests direction */
+#define OTX_APER_FLAG_TRANSFORM 8 /* apply `aper_to_local` before the test   */
+
+#define OTX_RULE_NONE 0
+#define OTX_RULE_CONSTANT 1    /* optika/rulings/_spacing.py:45  */
+#define OTX_RULE_POLY1D 2      /* optika/rulings/_spacing.py:78  */
+#define OTX_RULE_HOLOGRAPHIC 3 /* optika/rulings/_spacing.py:132 */
+
+#define OTX_SYS_FLAG_FINAL_IDENTITY 1 /* final_to_output is the identity */
+
+#define OTX_INPUT_RAYS 0         /* full ray state, optika/surfaces.py:123     */
+#define OTX_INPUT_GRID_INFINITY 1 /* object at infinity, _sequential.py:802-806 */
+#define OTX_INPUT_GRID_FINITE 2   /* finite object,      _sequential.py:807-809 */
+
+/* ---- descriptors ----------------------------------------------------- */
+
+/* Rigid affine map x' = m x + (t_hi + t_lo).  Composed on the host in
+ * float64 and split into a float-float translation so that the large
+ * offsets between surfaces are added without rounding. */
+typedef struct otx_affine {
+  float m[9]; /* row-major 3x3 rotation */
+  float t_hi[3];
+  float t_lo[3];
+} otx_affine; /* 60 bytes */
+
+/* Complex refractive index source of one layer or substrate.  A negative
+ * `table` means the constant n_re + i n_im; otherwise the index of a
+ * (wavelength, n, k) table in otx_system.tables, linearly interpolated and
+ * clamped at the ends (optika/chemicals/_chemicals.py:138-142). */
+typedef struct otx_layer {
+  float n_re;
+  float n_im;
+  float thickness; /* nm */
+  int32_t table;
+} otx_layer;
+
+/* A multilayer stack: `pre` layers, then `per` layers repeated
+ * `num_periods` times, then `post` layers, on the substrate layer
+ * (optika/materials/_layers.py:473-499, 611-645). */
+typedef struct otx_stack {
+  int32_t pre_begin, pre_count;
+  int32_t per_begin, per_count, num_periods;
+  int32_t post_begin, post_count;
+  int32_t substrate; /* layer index, or -1 for vacuum */
+} otx_stack;
+
+typedef struct otx_table {
+  int32_t offset; /* into otx_system.table_data: [wl(n), n(n), k(n)] */
+  int32_t count;
+} otx_table;
+
+typedef struct otx_surface {
+  otx_affine to_local;  /* previous frame -> this surface's frame        */
+  otx_affine to_output; /* this surface's frame -> output frame          */
+  otx_affine aper_to_local; /* surface frame -> aperture frame             */
+  otx_affine rule_xform;    /* polynomial-spacing argument transformation */
+
+  /* sag */
+  int32_t sag_type;
+  float sag_radius;    /* R (sphere), 2f (parabola)                          */
+  float sag_curvature; /* c = 1/R (sphere, conic, toroid minor radius)       */
+  float sag_conic;     /* k                                                  */
+  float sag_radius_of_rotation; /* toroid major radius                       */
+  float sag_focal_length;       /* parabola                                  */
+
+  /* material */
+  int32_t mat_type;
+  int32_t mat_is_mirror;
+  int32_t mat_stack; /* index into otx_system.stacks (multilayer types)      */
+  float sellmeier_b[3];
+  float sellmeier_c[3]; /* nm^2 */
+
+  /* aperture */
+  int32_t aper_type;
+  int32_t aper_flags;
+  float aper_p[4]; /* circular: r | rect: hx,hy | ellipse: rx,ry |
+                      sector: r, start, stop */
+  int32_t aper_vertex_begin, aper_vertex_count;
+
+  /* rulings */
+  int32_t rule_type;
+  int32_t rule_num_terms;
+  float rule_order;      /* diffraction order m                         */
+  float rule_efficiency; /* 1 for ideal rulings                          */
+  float rule_normal[3];  /* unit normal of the ruling planes             */
+  float rule_coef[OTX_MAX_POLY_TERMS]; /* d(x) = sum coef[k] x^k (mm)    */
+  float holo_x1[3], holo_x2[3];
+  float holo_wavelength; /* mm */
+  float holo_d1, holo_d2; /* +1 diverging, -1 converging */
+
+  int32_t is_sensor; /* bin rays leaving this surface (must be the last) */
+  int32_t pad_;
+} otx_surface;
+
+typedef struct otx_sensor {
+  int32_t num_x, num_y, num_w; /* pixels along x, y; wavelength bins    */
+  int32_t pad_;
+  float lo_x, lo_y;  /* lower edges (mm)                                */
+  float width_x, width_y; /* pixel pitch (mm)                           */
+  float w_lo, w_hi;  /* wavelength edges (nm), num_w uniform bins       */
+  float inv_width_x, inv_width_y; /* 1 / pitch (derived by the library) */
+  float inv_width_w;              /* num_w / (w_hi - w_lo) (derived)    */
+  int32_t pad2_;
+} otx_sensor;
+
+typedef struct otx_system {
+  int32_t abi_version;
+  int32_t num_surfaces;
+  int32_t input_mode; /* OTX_INPUT_*                                      */
+  int32_t newton_iterations; /* max toroid Newton steps (0 = default 12) */
+  int32_t flags;              /* OTX_SYS_FLAG_*                          */
+  int32_t pad_;
+  otx_affine final_to_output; /* last surface frame -> final output frame */
+  otx_sensor sensor;
+  otx_surface surfaces[OTX_MAX_SURFACES];
+  float vertices[2 * OTX_MAX_VERTICES]; /* polygon apertures (x,y pairs) */
+  otx_layer layers[OTX_MAX_LAYERS];
+  otx_stack stacks[OTX_MAX_STACKS];
+  otx_table tables[OTX_MAX_STACKS * 4];
+  uint64_t table_data; /* device pointer to float table storage          */
+} otx_system;
+
+/* Structure-of-arrays ray buffers (device pointers).  Any pointer may be
+ * null: an input then takes the reference's default (intensity 1,
+ * attenuation 0, index 1, unvignetted true), an output is not written.
+ * `stride_*` of 0 broadcasts element 0 (a scalar input). */
+typedef struct otx_rays {
+  uint64_t px, py, pz;      /* float* */
+  uint64_t dx, dy, dz;      /* float* */
+  uint64_t wavelength;      /* float* nm */
+  uint64_t intensity;       /* float*    */
+  uint64_t attenuation;     /* float* 1/mm */
+  uint64_t index_refraction;/* float*    */
+  uint64_t unvignetted;     /* uint8_t*  */
+  uint64_t opl;             /* double*   optical path length (mm)       */
+  int64_t count;
+  int64_t surface_stride;   /* elements between surfaces when accumulating */
+} otx_rays;
+
+/* Grid inputs of SequentialSystem.raytrace (float* device arrays, each
+ * with its own element stride, 0 = broadcast). */
+typedef struct otx_grid {
+  uint64_t wavelength, field_x, field_y, pupil_x, pupil_y, intensity;
+  int64_t stride_wavelength, stride_field, stride_pupil, stride_intensity;
+  int64_t count;
+} otx_grid;
+
+typedef struct otx_image {
+  uint64_t counts; /* uint32_t[num_w][num_x][num_y] or 0 */
+  uint64_t flux;   /* float   [num_w][num_x][num_y] or 0 */
+} otx_image;
+
+typedef struct otx_launch {
+  int32_t rays_per_thread; /* 1, 2 or 4; 0 = library default          */
+  int32_t block_size;      /* threads per CTA; 0 = library default     */
+  int32_t accumulate;      /* 1: write every surface's rays            */
+  int32_t pad_;
+} otx_launch;
+
+/* ---- entry points ---------------------------------------------------- */
+
+/* ABI self-description: sizes of the descriptor structs, for binding
+ * checks.  `which`: 0 otx_system, 1 otx_surface, 2 otx_rays, 3 otx_grid,
+ * 4 otx_image, 5 otx_launch, 6 otx_affine, 7 otx_sensor. */
+int64_t otx_sizeof(int32_t which);
+int32_t otx_abi_version(void);
+const char* otx_status_string(otx_status s);
+
+/* Trace a ray ensemble through every surface of `sys`.
+ * Replaces optika/propagators.py:19-41 (propagate_rays) and :44-73
+ * (accumulate_rays, when launch->accumulate), which loop
+ * optika/surfaces.py:123-198 (AbstractSurface.propagate_rays) per surface.
+ * `in` is in the frame the first surface's `to_local` maps from. */
+otx_status otx_trace_rays(const otx_system* sys, const otx_rays* in,
+                          const otx_rays* out, const otx_image* image,
+                          const otx_launch* launch, void* stream);
+
+/* Build input rays from (wavelength, field, pupil) and trace them.
+ * Replaces optika/systems/_sequential.py:791-828 (_calc_rayfunction_input)
+ * followed by :836-925 (raytrace) or :927-988 (rayfunction); sensor binning
+ * replaces optika/sensors/_sensors.py:92-161 (collect, image histogram). */
+otx_status otx_trace_grid(const otx_system* sys, const otx_grid* in,
+                          const otx_rays* out, const otx_image* image,
+                          const otx_launch* launch, void* stream);
+
+/* Multilayer reflectivity / transmissivity of `count` samples.
+ * Replaces optika/materials/_multilayers.py:240-532 (multilayer_efficiency).
+ * wavelength (nm), cos_incidence (direction), n_ambient (re, im) are float*
+ * device arrays with strides (0 = broadcast); stack_index (int32*, may be
+ * null = stack 0) selects one of sys->stacks per sample.  Outputs R_s, R_p,
+ * T_s, T_p (float*, any may be null). */
+otx_status otx_multilayer_efficiency(
+    const otx_system* sys, int64_t count, const float* wavelength,
+    int64_t stride_wavelength, const float* cos_incidence, int64_t stride_cos,
+    const float* n_re, const float* n_im, int64_t stride_n,
+    const int32_t* stack_index, float* r_s, float* r_p, float* t_s,
+    float* t_p, void* stream);
+
+/* Bin rays given in the sensor's local frame into count and flux images.
+ * Replaces optika/sensors/_sensors.py:92-161 (ImagingSensor.collect, the
+ * intensity-weighted na.histogram of position.xy and wavelength).  Reads
+ * px, py, wavelength (when wavelength bins are set), intensity and
+ * unvignetted of `rays`. */
+otx_status otx_collect(const otx_sensor* sensor, const otx_rays* rays,
+                       const otx_image* image, void* stream);
+
+/* Evaluate the sag of sys->surfaces[0] at `in` positions.
+ * mode 0: sag z(x, y) into out->pz   (optika/sags/_abc.py:48-62 __call__)
+ * mode 1: unit normal into out->d*   (optika/sags/_abc.py:64-75 normal)
+ * mode 2: intercept of the rays (in->p*, in->d*) into out->p*
+ *         (optika/sags/_abc.py:76-107 intercept and its overrides). */
+otx_status otx_sag_eval(const otx_system* sys, int32_t mode, const otx_rays* in,
+                        const otx_rays* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPTIKA_GB300_H */

@@ -1,0 +1,382 @@
+"""GPU calls behind the host API: tensors in, C-ABI call, tensors out.
+
+Every public entry point of the package that computes something ends here,
+in a call through the C-ABI library.  There is no CPU path: without a CUDA
+device these functions raise.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import Sequence
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from ._lower import lower_surfaces
+from .rays import RayFunctionArray, RayVectorArray
+from .transforms import matrix_of, rigid_inverse
+from .vectors import Cartesian3dVectorArray, PolarizationVectorArray
+
+
+def device() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("optika_gb300 needs a CUDA device (GB300, sm_103a); none is available")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream_handle() -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def ptr(t: torch.Tensor | None) -> int:
+    return 0 if t is None else t.data_ptr()
+
+
+def as_f32(x, dev) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        return x.to(device=dev, dtype=torch.float32)
+    return torch.as_tensor(np.asarray(x, dtype=np.float32), device=dev)
+
+
+class _Field:
+    """A flattened float32 device input with its element stride (0 = scalar)."""
+
+    def __init__(self, t: torch.Tensor, n: int):
+        if t.numel() == 1:
+            self.t = t.reshape(1).contiguous()
+            self.stride = 0
+        else:
+            self.t = t.reshape(-1).contiguous()
+            if self.t.numel() != n:
+                raise ValueError("input sizes do not broadcast")
+            self.stride = 1
+
+
+def _broadcast_inputs(values: Sequence, dev) -> tuple[list[_Field], tuple[int, ...]]:
+    ts = [as_f32(v, dev) for v in values]
+    shape = torch.broadcast_shapes(*[t.shape for t in ts])
+    n = int(np.prod(shape)) if len(shape) else 1
+    out = []
+    for t in ts:
+        if t.numel() == 1:
+            out.append(_Field(t, n))
+        else:
+            out.append(_Field(t.expand(shape), n))
+    return out, tuple(shape)
+
+
+def _alloc_rays(n: int, dev, shape_prefix: tuple = (), fields=None) -> dict[str, torch.Tensor]:
+    full = shape_prefix + (n,)
+    names = ("px", "py", "pz", "dx", "dy", "dz", "wavelength", "intensity", "attenuation",
+             "index_refraction", "unvignetted", "opl")
+    out = {}
+    for k in names:
+        if fields is not None and k not in fields:
+            out[k] = None
+        elif k == "unvignetted":
+            out[k] = torch.empty(full, dtype=torch.uint8, device=dev)
+        elif k == "opl":
+            out[k] = torch.empty(full, dtype=torch.float64, device=dev)
+        else:
+            out[k] = torch.empty(full, dtype=torch.float32, device=dev)
+    return out
+
+
+def _rays_struct(b: dict, n: int, stride: int = 0) -> L.Rays:
+    r = L.Rays()
+    for k in ("px", "py", "pz", "dx", "dy", "dz", "wavelength", "intensity", "attenuation",
+              "index_refraction", "unvignetted", "opl"):
+        setattr(r, k, ptr(b.get(k)))
+    r.count = n
+    r.surface_stride = stride
+    return r
+
+
+def _to_ray_array(b: dict, shape: tuple) -> RayVectorArray:
+    def rs(t):
+        return t.reshape(t.shape[:-1] + shape)
+
+    return RayVectorArray(
+        wavelength=rs(b["wavelength"]),
+        position=Cartesian3dVectorArray(rs(b["px"]), rs(b["py"]), rs(b["pz"])),
+        direction=Cartesian3dVectorArray(rs(b["dx"]), rs(b["dy"]), rs(b["dz"])),
+        intensity=rs(b["intensity"]),
+        attenuation=rs(b["attenuation"]),
+        index_refraction=rs(b["index_refraction"]),
+        unvignetted=rs(b["unvignetted"]).bool(),
+        opl=rs(b["opl"]),
+    )
+
+
+def _image_buffers(sensor, wavelength_bins, dev):
+    nx, ny = sensor.num_pixel
+    nw = 1 if wavelength_bins is None else int(wavelength_bins[2])
+    counts = torch.zeros((nw, int(nx), int(ny)), dtype=torch.int32, device=dev)
+    flux = torch.zeros((nw, int(nx), int(ny)), dtype=torch.float32, device=dev)
+    img = L.Image()
+    img.counts = counts.data_ptr()
+    img.flux = flux.data_ptr()
+    return counts, flux, img
+
+
+# ---------------------------------------------------------------- traces
+
+
+OUTPUT_FIELDS = ("px", "py", "pz", "dx", "dy", "dz", "wavelength", "intensity", "attenuation",
+                 "index_refraction", "unvignetted", "opl")
+
+
+class PreparedTrace:
+    """A grid trace with its descriptor and every buffer allocated once.
+
+    ``run()`` enqueues exactly one kernel (plus the image clear when binning)
+    on the current stream, so it can be timed, repeated or captured in a
+    CUDA graph.  ``outputs`` selects which ray fields are written.
+    """
+
+    def __init__(self, system, *, wavelength, field, pupil, intensity=None, accumulate=False,
+                 final_local=True, image=False, wavelength_bins=None, launch=None,
+                 outputs=OUTPUT_FIELDS):
+        dev = device()
+        self.device = dev
+        surfaces = system.surfaces_all
+        obj = system.object
+        pre = rigid_inverse(matrix_of(system.transformation)) @ (
+            matrix_of(obj.transformation) if obj is not None else np.eye(4)
+        )
+        sensor = system.sensor
+        if final_local:
+            if sensor is None:
+                raise ValueError("rayfunction needs a sensor")
+            final = rigid_inverse(matrix_of(sensor.transformation)) @ matrix_of(
+                surfaces[-1].transformation
+            )
+        else:
+            final = None
+        mode = L.INPUT_GRID_INFINITY if system.object_is_at_infinity else L.INPUT_GRID_FINITE
+        self.lowering = lower_surfaces(
+            surfaces, pre=pre, final=final, input_mode=mode,
+            sensor=sensor if image else None, wavelength_bins=wavelength_bins, device=dev,
+        )
+        vals = [wavelength, field.x, field.y, pupil.x, pupil.y]
+        if intensity is not None:
+            vals.append(intensity)
+        fields, shape = _broadcast_inputs(vals, dev)
+        n = int(np.prod(shape)) if len(shape) else 1
+        if fields[1].stride != fields[2].stride or fields[3].stride != fields[4].stride:
+            for f in fields[1:5]:
+                if f.stride == 0:
+                    f.t = f.t.expand(n).contiguous()
+                    f.stride = 1
+        g = L.Grid()
+        g.wavelength, g.field_x, g.field_y, g.pupil_x, g.pupil_y = (ptr(f.t) for f in fields[:5])
+        g.stride_wavelength = fields[0].stride
+        g.stride_field = fields[1].stride
+        g.stride_pupil = fields[3].stride
+        if intensity is not None:
+            g.intensity = ptr(fields[5].t)
+            g.stride_intensity = fields[5].stride
+        g.count = n
+        self.grid = g
+        self.fields = fields
+        self.shape = shape
+        self.count = n
+        self.num_surfaces = len(surfaces)
+        self.accumulate = accumulate
+        self.bufs = _alloc_rays(n, dev, (self.num_surfaces,) if accumulate else (), outputs)
+        self.out = _rays_struct(self.bufs, n, n if accumulate else 0)
+        self.img = L.Image()
+        self.counts = self.flux = None
+        if image:
+            self.counts, self.flux, self.img = _image_buffers(sensor, wavelength_bins, dev)
+        self.launch_desc = launch if launch is not None else L.Launch()
+        self.launch_desc.accumulate = 1 if accumulate else 0
+        self.lib = L.load()
+
+    def run(self) -> None:
+        if self.counts is not None:
+            self.counts.zero_()
+            self.flux.zero_()
+        st = self.lib.otx_trace_grid(
+            ctypes.byref(self.lowering.sys), ctypes.byref(self.grid), ctypes.byref(self.out),
+            ctypes.byref(self.img), ctypes.byref(self.launch_desc), stream_handle(),
+        )
+        L.check(st, "otx_trace_grid")
+
+    def result(self) -> RayFunctionArray:
+        b = {k: (v if v is not None else None) for k, v in self.bufs.items()}
+        rays = _to_ray_array_partial(b, self.shape)
+        img = (self.counts, self.flux) if self.counts is not None else None
+        return RayFunctionArray(inputs=None, outputs=rays, image=img)
+
+
+def _to_ray_array_partial(b: dict, shape: tuple) -> RayVectorArray:
+    def rs(t):
+        return None if t is None else t.reshape(t.shape[:-1] + shape)
+
+    unv = rs(b["unvignetted"])
+    return RayVectorArray(
+        wavelength=rs(b["wavelength"]),
+        position=Cartesian3dVectorArray(rs(b["px"]), rs(b["py"]), rs(b["pz"])),
+        direction=Cartesian3dVectorArray(rs(b["dx"]), rs(b["dy"]), rs(b["dz"])),
+        intensity=rs(b["intensity"]),
+        attenuation=rs(b["attenuation"]),
+        index_refraction=rs(b["index_refraction"]),
+        unvignetted=None if unv is None else unv.bool(),
+        opl=rs(b["opl"]),
+    )
+
+
+def trace_grid(system, *, wavelength, field, pupil, intensity=None, accumulate: bool,
+               final_local: bool, image: bool = False, wavelength_bins=None,
+               launch: L.Launch | None = None, outputs=OUTPUT_FIELDS) -> RayFunctionArray:
+    """Input rays from (wavelength, field, pupil), traced through
+    ``system.surfaces_all`` (optika/systems/_sequential.py:791-988)."""
+    p = PreparedTrace(system, wavelength=wavelength, field=field, pupil=pupil,
+                      intensity=intensity, accumulate=accumulate, final_local=final_local,
+                      image=image, wavelength_bins=wavelength_bins, launch=launch,
+                      outputs=outputs)
+    p.run()
+    return p.result()
+
+
+def _rays_inputs(rays: RayVectorArray, dev) -> tuple[dict, tuple, int]:
+    comps = dict(
+        px=rays.position.x,
+        py=rays.position.y,
+        pz=rays.position.z,
+        dx=rays.direction.x,
+        dy=rays.direction.y,
+        dz=rays.direction.z,
+        wavelength=rays.wavelength if rays.wavelength is not None else 0.0,
+        intensity=rays.intensity,
+        attenuation=rays.attenuation,
+        index_refraction=rays.index_refraction,
+    )
+    ts = {k: as_f32(v, dev) for k, v in comps.items()}
+    unv = rays.unvignetted
+    unv_t = (unv.to(dev) if isinstance(unv, torch.Tensor) else torch.as_tensor(np.asarray(unv), device=dev))
+    opl = rays.opl
+    opl_t = (opl.to(device=dev, dtype=torch.float64) if isinstance(opl, torch.Tensor)
+             else torch.as_tensor(np.asarray(opl, dtype=np.float64), device=dev))
+    shape = torch.broadcast_shapes(*[t.shape for t in ts.values()], unv_t.shape, opl_t.shape)
+    n = int(np.prod(shape)) if len(shape) else 1
+    b = {k: t.expand(shape).reshape(-1).contiguous() for k, t in ts.items()}
+    b["unvignetted"] = unv_t.expand(shape).reshape(-1).to(torch.uint8).contiguous()
+    b["opl"] = opl_t.expand(shape).reshape(-1).contiguous()
+    return b, tuple(shape), n
+
+
+def propagate_rays(surfaces: Sequence, rays: RayVectorArray, accumulate: bool = False,
+                   launch: L.Launch | None = None) -> RayVectorArray:
+    """optika/propagators.py:19-73 over the given surfaces, on the GPU."""
+    dev = device()
+    b_in, shape, n = _rays_inputs(rays, dev)
+    lw = lower_surfaces(list(surfaces), pre=np.eye(4), final=None, input_mode=L.INPUT_RAYS,
+                        device=dev)
+    S = len(surfaces)
+    bufs = _alloc_rays(n, dev, (S,) if accumulate else ())
+    ln = launch if launch is not None else L.Launch()
+    ln.accumulate = 1 if accumulate else 0
+    lib = L.load()
+    st = lib.otx_trace_rays(
+        ctypes.byref(lw.sys), ctypes.byref(_rays_struct(b_in, n)),
+        ctypes.byref(_rays_struct(bufs, n, n if accumulate else 0)), None, ctypes.byref(ln),
+        stream_handle(),
+    )
+    L.check(st, "otx_trace_rays")
+    return _to_ray_array(bufs, shape)
+
+
+def collect(sensor, rays: RayVectorArray, wavelength=None, where=True):
+    """optika/sensors/_sensors.py:92-161 on the GPU: (counts, flux) images."""
+    dev = device()
+    b_in, shape, n = _rays_inputs(rays, dev)
+    if where is not True:
+        w = torch.as_tensor(np.asarray(where) if not isinstance(where, torch.Tensor) else where,
+                            device=dev).expand(shape).reshape(-1)
+        b_in["unvignetted"] = (b_in["unvignetted"].bool() & w.bool()).to(torch.uint8)
+    lw = lower_surfaces([sensor], pre=np.eye(4), final=None, input_mode=L.INPUT_RAYS,
+                        sensor=sensor, wavelength_bins=wavelength)
+    counts, flux, img = _image_buffers(sensor, wavelength, dev)
+    lib = L.load()
+    st = lib.otx_collect(ctypes.byref(lw.sys.sensor), ctypes.byref(_rays_struct(b_in, n)),
+                         ctypes.byref(img), stream_handle())
+    L.check(st, "otx_collect")
+    return counts, flux
+
+
+def _sag_system(sag) -> L.System:
+    from .surfaces import Surface
+
+    return lower_surfaces([Surface(sag=sag)], pre=np.eye(4), final=None,
+                          input_mode=L.INPUT_RAYS).sys
+
+
+def sag_eval(sag, what: str, position):
+    dev = device()
+    fields, shape = _broadcast_inputs([position.x, position.y], dev)
+    n = int(np.prod(shape)) if len(shape) else 1
+    x = fields[0].t.expand(n).contiguous() if fields[0].stride == 0 else fields[0].t
+    y = fields[1].t.expand(n).contiguous() if fields[1].stride == 0 else fields[1].t
+    inp = _rays_struct(dict(px=x, py=y), n)
+    lib = L.load()
+    sys_ = _sag_system(sag)
+    if what == "sag":
+        z = torch.empty(n, dtype=torch.float32, device=dev)
+        out = _rays_struct(dict(pz=z), n)
+        L.check(lib.otx_sag_eval(ctypes.byref(sys_), 0, ctypes.byref(inp), ctypes.byref(out),
+                                 stream_handle()), "otx_sag_eval")
+        return z.reshape(shape)
+    nx, ny, nz = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
+    out = _rays_struct(dict(dx=nx, dy=ny, dz=nz), n)
+    L.check(lib.otx_sag_eval(ctypes.byref(sys_), 1, ctypes.byref(inp), ctypes.byref(out),
+                             stream_handle()), "otx_sag_eval")
+    return Cartesian3dVectorArray(nx.reshape(shape), ny.reshape(shape), nz.reshape(shape))
+
+
+def sag_intercept(sag, rays: RayVectorArray) -> RayVectorArray:
+    dev = device()
+    b_in, shape, n = _rays_inputs(rays, dev)
+    px, py, pz = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
+    out = _rays_struct(dict(px=px, py=py, pz=pz), n)
+    lib = L.load()
+    sys_ = _sag_system(sag)
+    L.check(lib.otx_sag_eval(ctypes.byref(sys_), 2, ctypes.byref(_rays_struct(b_in, n)),
+                             ctypes.byref(out), stream_handle()), "otx_sag_eval")
+    res = _to_ray_array({**b_in, "px": px, "py": py, "pz": pz}, shape)
+    return res
+
+
+def multilayer_efficiency_gpu(wavelength, direction, n, layers, substrate):
+    dev = device()
+    from ._lower import Lowering
+
+    lw = Lowering()
+    lw.add_stack(layers, substrate)
+    lw.finish_tables(dev)
+    n_arr = np.asarray(n) if not isinstance(n, torch.Tensor) else n
+    if isinstance(n_arr, torch.Tensor):
+        n_re, n_im = n_arr.real if n_arr.is_complex() else n_arr, (
+            n_arr.imag if n_arr.is_complex() else torch.zeros_like(n_arr))
+    else:
+        n_re, n_im = np.real(n_arr), np.imag(n_arr)
+    fields, shape = _broadcast_inputs([wavelength, direction, n_re, n_im], dev)
+    cnt = int(np.prod(shape)) if len(shape) else 1
+    if fields[2].stride != fields[3].stride:
+        for f in fields[2:4]:
+            if f.stride == 0:
+                f.t = f.t.expand(cnt).contiguous()
+                f.stride = 1
+    outs = [torch.empty(cnt, dtype=torch.float32, device=dev) for _ in range(4)]
+    lib = L.load()
+    st = lib.otx_multilayer_efficiency(
+        ctypes.byref(lw.sys), cnt, ptr(fields[0].t), fields[0].stride, ptr(fields[1].t),
+        fields[1].stride, ptr(fields[2].t), ptr(fields[3].t), fields[2].stride, None,
+        *(ptr(o) for o in outs), stream_handle(),
+    )
+    L.check(st, "otx_multilayer_efficiency")
+    rs, rp, ts, tp = (o.reshape(shape) for o in outs)
+    return PolarizationVectorArray(rs, rp), PolarizationVectorArray(ts, tp)

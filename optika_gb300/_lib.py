@@ -1,0 +1,281 @@
+"""ctypes binding of the C-ABI in ``include/optika_gb300.h``.
+
+The structures below mirror the header field for field; ``check_layout``
+compares their sizes with ``otx_sizeof`` exported by the library.  Loading
+fails loudly when the library has not been built: there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import pathlib
+
+ABI_VERSION = 1
+MAX_SURFACES = 16
+MAX_POLY_TERMS = 8
+MAX_VERTICES = 64
+MAX_LAYERS = 64
+MAX_STACKS = 4
+
+OK = 0
+ERR_INVALID = 1
+ERR_UNSUPPORTED = 2
+ERR_CUDA = 3
+ERR_SIZE = 4
+ERR_TIMEOUT = 5
+
+SAG_FLAT, SAG_SPHERE, SAG_CONIC, SAG_PARABOLA, SAG_TOROID = range(5)
+MAT_VACUUM, MAT_MIRROR, MAT_GLASS, MAT_MULTILAYER_MIRROR, MAT_MULTILAYER_FILM = range(5)
+APER_NONE, APER_CIRCULAR, APER_RECTANGULAR, APER_ELLIPTICAL, APER_SECTOR, APER_POLYGON = range(6)
+APER_FLAG_INVERTED = 1
+APER_FLAG_ACTIVE = 2
+APER_FLAG_DIRECTION = 4
+APER_FLAG_TRANSFORM = 8
+RULE_NONE, RULE_CONSTANT, RULE_POLY1D, RULE_HOLOGRAPHIC = range(4)
+INPUT_RAYS, INPUT_GRID_INFINITY, INPUT_GRID_FINITE = range(3)
+SYS_FLAG_FINAL_IDENTITY = 1
+
+f32 = ctypes.c_float
+i32 = ctypes.c_int32
+i64 = ctypes.c_int64
+u64 = ctypes.c_uint64
+
+
+class Affine(ctypes.Structure):
+    _fields_ = [("m", f32 * 9), ("t_hi", f32 * 3), ("t_lo", f32 * 3)]
+
+
+class Layer(ctypes.Structure):
+    _fields_ = [("n_re", f32), ("n_im", f32), ("thickness", f32), ("table", i32)]
+
+
+class Stack(ctypes.Structure):
+    _fields_ = [
+        ("pre_begin", i32),
+        ("pre_count", i32),
+        ("per_begin", i32),
+        ("per_count", i32),
+        ("num_periods", i32),
+        ("post_begin", i32),
+        ("post_count", i32),
+        ("substrate", i32),
+    ]
+
+
+class Table(ctypes.Structure):
+    _fields_ = [("offset", i32), ("count", i32)]
+
+
+class Surface(ctypes.Structure):
+    _fields_ = [
+        ("to_local", Affine),
+        ("to_output", Affine),
+        ("aper_to_local", Affine),
+        ("rule_xform", Affine),
+        ("sag_type", i32),
+        ("sag_radius", f32),
+        ("sag_curvature", f32),
+        ("sag_conic", f32),
+        ("sag_radius_of_rotation", f32),
+        ("sag_focal_length", f32),
+        ("mat_type", i32),
+        ("mat_is_mirror", i32),
+        ("mat_stack", i32),
+        ("sellmeier_b", f32 * 3),
+        ("sellmeier_c", f32 * 3),
+        ("aper_type", i32),
+        ("aper_flags", i32),
+        ("aper_p", f32 * 4),
+        ("aper_vertex_begin", i32),
+        ("aper_vertex_count", i32),
+        ("rule_type", i32),
+        ("rule_num_terms", i32),
+        ("rule_order", f32),
+        ("rule_efficiency", f32),
+        ("rule_normal", f32 * 3),
+        ("rule_coef", f32 * MAX_POLY_TERMS),
+        ("holo_x1", f32 * 3),
+        ("holo_x2", f32 * 3),
+        ("holo_wavelength", f32),
+        ("holo_d1", f32),
+        ("holo_d2", f32),
+        ("is_sensor", i32),
+        ("pad_", i32),
+    ]
+
+
+class Sensor(ctypes.Structure):
+    _fields_ = [
+        ("num_x", i32),
+        ("num_y", i32),
+        ("num_w", i32),
+        ("pad_", i32),
+        ("lo_x", f32),
+        ("lo_y", f32),
+        ("width_x", f32),
+        ("width_y", f32),
+        ("w_lo", f32),
+        ("w_hi", f32),
+        ("inv_width_x", f32),
+        ("inv_width_y", f32),
+        ("inv_width_w", f32),
+        ("pad2_", i32),
+    ]
+
+
+class System(ctypes.Structure):
+    _fields_ = [
+        ("abi_version", i32),
+        ("num_surfaces", i32),
+        ("input_mode", i32),
+        ("newton_iterations", i32),
+        ("flags", i32),
+        ("pad_", i32),
+        ("final_to_output", Affine),
+        ("sensor", Sensor),
+        ("surfaces", Surface * MAX_SURFACES),
+        ("vertices", f32 * (2 * MAX_VERTICES)),
+        ("layers", Layer * MAX_LAYERS),
+        ("stacks", Stack * MAX_STACKS),
+        ("tables", Table * (MAX_STACKS * 4)),
+        ("table_data", u64),
+    ]
+
+
+class Rays(ctypes.Structure):
+    _fields_ = [
+        ("px", u64),
+        ("py", u64),
+        ("pz", u64),
+        ("dx", u64),
+        ("dy", u64),
+        ("dz", u64),
+        ("wavelength", u64),
+        ("intensity", u64),
+        ("attenuation", u64),
+        ("index_refraction", u64),
+        ("unvignetted", u64),
+        ("opl", u64),
+        ("count", i64),
+        ("surface_stride", i64),
+    ]
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [
+        ("wavelength", u64),
+        ("field_x", u64),
+        ("field_y", u64),
+        ("pupil_x", u64),
+        ("pupil_y", u64),
+        ("intensity", u64),
+        ("stride_wavelength", i64),
+        ("stride_field", i64),
+        ("stride_pupil", i64),
+        ("stride_intensity", i64),
+        ("count", i64),
+    ]
+
+
+class Image(ctypes.Structure):
+    _fields_ = [("counts", u64), ("flux", u64)]
+
+
+class Launch(ctypes.Structure):
+    _fields_ = [
+        ("rays_per_thread", i32),
+        ("block_size", i32),
+        ("accumulate", i32),
+        ("pad_", i32),
+    ]
+
+
+LAYOUT = {
+    0: System,
+    1: Surface,
+    2: Rays,
+    3: Grid,
+    4: Image,
+    5: Launch,
+    6: Affine,
+    7: Sensor,
+    8: Layer,
+    9: Stack,
+}
+
+LIB_PATH = pathlib.Path(__file__).resolve().parent / "_lib" / "liboptika_gb300.so"
+
+_lib = None
+
+
+class OtxError(RuntimeError):
+    """A non-zero ``otx_status`` returned by the library."""
+
+    def __init__(self, status: int, where: str):
+        self.status = status
+        msg = _status_string(status)
+        super().__init__(f"{where} failed with status {status} ({msg})")
+
+
+def _status_string(status: int) -> str:
+    if _lib is None:
+        return "library not loaded"
+    return _lib.otx_status_string(status).decode()
+
+
+def _declare(lib: ctypes.CDLL) -> None:
+    P = ctypes.POINTER
+    v = ctypes.c_void_p
+    lib.otx_sizeof.argtypes = [i32]
+    lib.otx_sizeof.restype = i64
+    lib.otx_abi_version.argtypes = []
+    lib.otx_abi_version.restype = i32
+    lib.otx_status_string.argtypes = [i32]
+    lib.otx_status_string.restype = ctypes.c_char_p
+    lib.otx_trace_rays.argtypes = [P(System), P(Rays), P(Rays), P(Image), P(Launch), v]
+    lib.otx_trace_rays.restype = i32
+    lib.otx_trace_grid.argtypes = [P(System), P(Grid), P(Rays), P(Image), P(Launch), v]
+    lib.otx_trace_grid.restype = i32
+    lib.otx_multilayer_efficiency.argtypes = [
+        P(System), i64, v, i64, v, i64, v, v, i64, v, v, v, v, v, v,
+    ]
+    lib.otx_multilayer_efficiency.restype = i32
+    lib.otx_collect.argtypes = [P(Sensor), P(Rays), P(Image), v]
+    lib.otx_collect.restype = i32
+    lib.otx_sag_eval.argtypes = [P(System), i32, P(Rays), P(Rays), v]
+    lib.otx_sag_eval.restype = i32
+
+
+def load() -> ctypes.CDLL:
+    """Load the C-ABI library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"optika_gb300 native library not found at {LIB_PATH}; "
+                "run `python -c 'import __graft_entry__ as g; g.build()'` "
+                "or `python -m optika_gb300.build` first"
+            )
+        lib = ctypes.CDLL(str(LIB_PATH))
+        _declare(lib)
+        if lib.otx_abi_version() != ABI_VERSION:
+            raise RuntimeError("optika_gb300 library ABI version mismatch; rebuild it")
+        _lib = lib
+        check_layout()
+    return _lib
+
+
+def check_layout() -> None:
+    """Compare every ctypes structure size with the C compiler's."""
+    lib = _lib if _lib is not None else load()
+    for which, cls in LAYOUT.items():
+        n = lib.otx_sizeof(which)
+        if n != ctypes.sizeof(cls):
+            raise RuntimeError(
+                f"ABI layout mismatch for {cls.__name__}: C {n} bytes, ctypes {ctypes.sizeof(cls)}"
+            )
+
+
+def check(status: int, where: str) -> None:
+    if status != OK:
+        raise OtxError(status, where)

@@ -1,0 +1,129 @@
+// Standalone sensor binning and sag evaluation, sharing the device functions
+// of the fused trace.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/optika_gb300.h"
+#include "trace_device.cuh"
+#include "trace_kernel_decl.h"
+
+namespace otx {
+
+__device__ __forceinline__ int64_t collect_bin(const otx_sensor& S, float x, float y,
+                                               float wl) {
+  const float hx = S.lo_x + S.num_x * S.width_x;
+  const float hy = S.lo_y + S.num_y * S.width_y;
+  if (!(x >= S.lo_x && x <= hx && y >= S.lo_y && y <= hy)) return -1;
+  int ix = (int)floorf((x - S.lo_x) * S.inv_width_x);
+  int iy = (int)floorf((y - S.lo_y) * S.inv_width_y);
+  ix = min(max(ix, 0), S.num_x - 1);
+  iy = min(max(iy, 0), S.num_y - 1);
+  int iw = 0;
+  if (S.w_hi > S.w_lo) {
+    if (!(wl >= S.w_lo && wl <= S.w_hi)) return -1;
+    iw = (int)floorf((wl - S.w_lo) * S.inv_width_w);
+    iw = min(max(iw, 0), S.num_w - 1);
+  }
+  return ((int64_t)iw * S.num_x + ix) * S.num_y + iy;
+}
+
+// optika/sensors/_sensors.py:92-161: histogram of position.xy (and
+// wavelength) weighted by intensity * unvignetted.
+__global__ void k_collect(const otx_sensor S, const otx_rays r, const otx_image img) {
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < r.count; i += step) {
+    if (r.unvignetted && reinterpret_cast<const uint8_t*>(r.unvignetted)[i] == 0) continue;
+    const float x = reinterpret_cast<const float*>(r.px)[i];
+    const float y = reinterpret_cast<const float*>(r.py)[i];
+    const float wl = r.wavelength ? reinterpret_cast<const float*>(r.wavelength)[i] : 0.f;
+    const int64_t b = collect_bin(S, x, y, wl);
+    if (b < 0) continue;
+    if (img.counts) atomicAdd(reinterpret_cast<unsigned int*>(img.counts) + b, 1u);
+    if (img.flux) {
+      const float w = r.intensity ? reinterpret_cast<const float*>(r.intensity)[i] : 1.f;
+      atomicAdd(reinterpret_cast<float*>(img.flux) + b, w);
+    }
+  }
+}
+
+// mode 0: sag z(x, y) -> out.pz ; 1: normal -> out.d* ; 2: intercept -> out.p*
+__global__ void k_sag(const __grid_constant__ otx_system sys, const int mode,
+                      const otx_rays in, const otx_rays out) {
+  const otx_surface& s = sys.surfaces[0];
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < in.count; i += step) {
+    const float x = reinterpret_cast<const float*>(in.px)[i];
+    const float y = reinterpret_cast<const float*>(in.py)[i];
+    if (mode == 0) {
+      float gx, gy;
+      float z = sag_eval(s, x, y, gx, gy);
+      reinterpret_cast<float*>(out.pz)[i] = z;
+    } else if (mode == 1) {
+      float nx, ny, nz;
+      normal(s, x, y, nx, ny, nz);
+      reinterpret_cast<float*>(out.dx)[i] = nx;
+      reinterpret_cast<float*>(out.dy)[i] = ny;
+      reinterpret_cast<float*>(out.dz)[i] = nz;
+    } else {
+      const float z0 = reinterpret_cast<const float*>(in.pz)[i];
+      const float ux = reinterpret_cast<const float*>(in.dx)[i];
+      const float uy = reinterpret_cast<const float*>(in.dy)[i];
+      const float uz = reinterpret_cast<const float*>(in.dz)[i];
+      const float lo[3] = {0.f, 0.f, 0.f};
+      float px, py, pz;
+      intercept(s, sys.newton_iterations, x, y, z0, lo, ux, uy, uz, px, py, pz);
+      reinterpret_cast<float*>(out.px)[i] = px;
+      reinterpret_cast<float*>(out.py)[i] = py;
+      reinterpret_cast<float*>(out.pz)[i] = pz;
+    }
+  }
+}
+
+static int grid_for(int64_t n) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 132;
+  int64_t need = (n + 255) / 256;
+  const int64_t cap = (int64_t)sms * 16;
+  return (int)(need < cap ? need : cap);
+}
+
+}  // namespace otx
+
+using namespace otx;
+
+extern "C" otx_status otx_collect(const otx_sensor* sensor, const otx_rays* rays,
+                                  const otx_image* image, void* stream) {
+  if (!sensor || !rays || !image || rays->count < 0) return OTX_ERR_INVALID;
+  if (sensor->num_x < 1 || sensor->num_y < 1 || sensor->num_w < 1) return OTX_ERR_INVALID;
+  if (!(sensor->width_x > 0.f) || !(sensor->width_y > 0.f)) return OTX_ERR_INVALID;
+  if (rays->count == 0) return OTX_OK;
+  if (!rays->px || !rays->py) return OTX_ERR_INVALID;
+  if (sensor->w_hi > sensor->w_lo && !rays->wavelength) return OTX_ERR_INVALID;
+  otx_sensor S = *sensor;
+  S.inv_width_x = 1.f / S.width_x;
+  S.inv_width_y = 1.f / S.width_y;
+  S.inv_width_w = (S.w_hi > S.w_lo) ? (float)S.num_w / (S.w_hi - S.w_lo) : 0.f;
+  k_collect<<<grid_for(rays->count), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      S, *rays, *image);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+extern "C" otx_status otx_sag_eval(const otx_system* sys, int32_t mode, const otx_rays* in,
+                                   const otx_rays* out, void* stream) {
+  if (!sys || sys->abi_version != OTX_ABI_VERSION || !in || !out) return OTX_ERR_INVALID;
+  if (mode < 0 || mode > 2) return OTX_ERR_INVALID;
+  const int st = sys->surfaces[0].sag_type;
+  if (st < OTX_SAG_FLAT || st > OTX_SAG_TOROID) return OTX_ERR_UNSUPPORTED;
+  if (in->count < 0) return OTX_ERR_INVALID;
+  if (in->count == 0) return OTX_OK;
+  if (!in->px || !in->py) return OTX_ERR_INVALID;
+  if (mode == 0 && !out->pz) return OTX_ERR_INVALID;
+  if (mode == 1 && (!out->dx || !out->dy || !out->dz)) return OTX_ERR_INVALID;
+  if (mode == 2 && (!in->pz || !in->dx || !in->dy || !in->dz || !out->px || !out->py || !out->pz))
+    return OTX_ERR_INVALID;
+  k_sag<<<grid_for(in->count), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*sys, mode, *in,
+                                                                               *out);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}

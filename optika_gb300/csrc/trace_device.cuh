@@ -1,0 +1,868 @@
+// Device functions of the fused sequential raytrace.
+//
+// Each function restates one step of optika's per-surface pipeline
+// (optika/surfaces.py:123-198) for one ray held in registers.  Arithmetic
+// is FP32; the frame changes between surfaces add their (large) translation
+// as a float-float pair so that positions near a surface stay accurate, and
+// every curved intercept ends with one Newton step evaluated in the
+// surface's own (small) coordinates.  The optical path length accumulates
+// as a float-float pair (FP64 throughput on GB300 is a small fraction of
+// FP32) and is stored as float64.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "../../include/optika_gb300.h"
+
+namespace otx {
+
+struct Ray {
+  float px, py, pz;      // position in the current frame (mm)
+  float dx, dy, dz;      // direction cosines
+  float wl;              // wavelength (nm)
+  float inten;           // intensity
+  float att;             // attenuation coefficient (1/mm)
+  float n;               // index of refraction of the current medium
+  bool ok;               // unvignetted
+  float opl_hi, opl_lo;  // optical path length (mm), float-float
+};
+
+// ---------------------------------------------------------------- helpers
+
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// opl += n t with the product split exactly by an FMA (Dekker's TwoProduct)
+// and the sum by TwoSum; the low parts are gathered in opl_lo.
+__device__ __forceinline__ void opl_add(Ray& r, float n, float t) {
+  const float p = n * t;
+  const float pe = fmaf(n, t, -p);
+  float s, e;
+  two_sum(r.opl_hi, p, s, e);
+  r.opl_hi = s;
+  r.opl_lo += e + pe;
+}
+
+__device__ __forceinline__ float sgnf(float x) {  // numpy.sign: 0 at 0
+  return (x > 0.f) ? 1.f : ((x < 0.f) ? -1.f : 0.f);
+}
+
+// Apply x' = m x + t to a position: the rotation in FP32, the translation
+// as a float-float add.  Returns the high part in (x,y,z) and the low part
+// in lo.
+__device__ __forceinline__ void affine_point(const otx_affine& f, float& x,
+                                             float& y, float& z, float lo[3]) {
+  float rx = fmaf(f.m[0], x, fmaf(f.m[1], y, f.m[2] * z));
+  float ry = fmaf(f.m[3], x, fmaf(f.m[4], y, f.m[5] * z));
+  float rz = fmaf(f.m[6], x, fmaf(f.m[7], y, f.m[8] * z));
+  float e;
+  two_sum(rx, f.t_hi[0], x, e);
+  lo[0] = e + f.t_lo[0];
+  two_sum(ry, f.t_hi[1], y, e);
+  lo[1] = e + f.t_lo[1];
+  two_sum(rz, f.t_hi[2], z, e);
+  lo[2] = e + f.t_lo[2];
+}
+
+__device__ __forceinline__ void rotate(const otx_affine& f, float& x, float& y,
+                                       float& z) {
+  float rx = fmaf(f.m[0], x, fmaf(f.m[1], y, f.m[2] * z));
+  float ry = fmaf(f.m[3], x, fmaf(f.m[4], y, f.m[5] * z));
+  float rz = fmaf(f.m[6], x, fmaf(f.m[7], y, f.m[8] * z));
+  x = rx;
+  y = ry;
+  z = rz;
+}
+
+// Full affine map of a position (high + low folded), used for outputs.
+__device__ __forceinline__ void affine_point_folded(const otx_affine& f,
+                                                    float& x, float& y,
+                                                    float& z) {
+  float lo[3];
+  affine_point(f, x, y, z, lo);
+  x += lo[0];
+  y += lo[1];
+  z += lo[2];
+}
+
+// ---------------------------------------------------------------- sags
+
+// Sag z(x, y) and its gradient for the curved sag types.
+// Conic: optika/sags/_conic.py:31-48 (sag), :50-75 (gradient c x / g).
+// Toroid: optika/sags/_toroidal.py:38-57 (sag), :59-88 (gradient).
+__device__ __forceinline__ float sag_eval(const otx_surface& s, float x,
+                                          float y, float& gx, float& gy) {
+  switch (s.sag_type) {
+    case OTX_SAG_SPHERE:
+    case OTX_SAG_CONIC:
+    case OTX_SAG_PARABOLA: {
+      const float c = s.sag_curvature;
+      const float kp1 = (s.sag_type == OTX_SAG_SPHERE) ? 1.f : 1.f + s.sag_conic;
+      const float r2 = fmaf(x, x, y * y);
+      const float g = sqrtf(1.f - kp1 * c * c * r2);
+      const float cg = c / g;
+      gx = cg * x;
+      gy = cg * y;
+      return c * r2 / (1.f + g);
+    }
+    case OTX_SAG_TOROID: {
+      const float c = s.sag_curvature;
+      const float r = s.sag_radius_of_rotation;
+      const float y2 = y * y;
+      const float g = sqrtf(1.f - c * c * y2);
+      const float zy = c * y2 / (1.f + g);
+      const float rz = r - zy;
+      const float f = sqrtf(fmaf(rz, rz, -x * x));
+      const float inv_f = 1.f / f;
+      gx = x * inv_f;
+      gy = rz * (c * y / g) * inv_f;
+      return r - f;
+    }
+    default:
+      gx = 0.f;
+      gy = 0.f;
+      return 0.f;
+  }
+}
+
+// One Newton step on f(t) = z(t) - sag(x(t), y(t)) from the current point.
+__device__ __forceinline__ float newton_step(const otx_surface& s, float& x,
+                                             float& y, float& z, float ux,
+                                             float uy, float uz) {
+  float gx, gy;
+  const float zs = sag_eval(s, x, y, gx, gy);
+  const float f = z - zs;
+  const float fp = uz - (gx * ux + gy * uy);
+  const float dt = f / fp;
+  x = fmaf(-dt, ux, x);
+  y = fmaf(-dt, uy, y);
+  z = fmaf(-dt, uz, z);
+  return dt;
+}
+
+// Intercept of the ray (origin o = hi + lo, direction u) with the sag.
+// On return (x,y,z) is the intercept in the surface frame and t the signed
+// distance along u from the origin.
+//
+// Root choice follows the reference for each type:
+//   flat      optika/sags/_flat.py:47-64
+//   sphere    optika/sags/_spherical.py:148-191 (root with -sign(r u_z))
+//   conic     optika/sags/_conic.py:77-170 (vertex-sheet root nearest o)
+//   parabola  optika/sags/_parabolic.py:65-158 (-sign(f u_z) root,
+//             linear form when u_x^2 + u_y^2 <= 1e-10)
+//   toroid    optika/sags/_abc.py:76-107 (iterative root near the vertex
+//             plane; here Newton from the plane intercept)
+// The closed forms use the cancellation-free product-of-roots identity.
+__device__ __forceinline__ float intercept(const otx_surface& s,
+                                           int newton_max, float ox, float oy,
+                                           float oz, const float lo[3],
+                                           float ux, float uy, float uz,
+                                           float& x, float& y, float& z) {
+  const float oxf = ox + lo[0], oyf = oy + lo[1], ozf = oz + lo[2];
+  if (s.sag_type == OTX_SAG_FLAT) {
+    const float inv = 1.f / uz;
+    const float t = -ozf * inv;
+    x = fmaf(t, ux, ox) + lo[0];
+    y = fmaf(t, uy, oy) + lo[1];
+    z = fmaf(t, uz, oz) + lo[2];
+    const float dt = z * inv;  // Newton step on z = 0
+    x = fmaf(-dt, ux, x);
+    y = fmaf(-dt, uy, y);
+    z = 0.f;
+    return t - dt;
+  }
+  float t;
+  switch (s.sag_type) {
+    case OTX_SAG_SPHERE: {
+      const float R = s.sag_radius;
+      // p = o - (0, 0, R); b = u.p; cc = |p|^2 - R^2 = |o|^2 - 2 o_z R
+      const float b = fmaf(ux, oxf, fmaf(uy, oyf, uz * (ozf - R)));
+      const float cc = fmaf(oxf, oxf, fmaf(oyf, oyf, ozf * (ozf - 2.f * R)));
+      const float q = sqrtf(fmaf(b, b, -cc));
+      const float sg = sgnf(R * uz);
+      // chosen root: -b - sg q ; the other root: -b + sg q ; product = cc
+      if (sg != 0.f && sgnf(-b) == sg)
+        t = cc / (-b + sg * q);
+      else
+        t = -b - sg * q;
+      break;
+    }
+    case OTX_SAG_CONIC: {
+      const float c = s.sag_curvature;
+      const float kp1 = 1.f + s.sag_conic;
+      const float A = c * fmaf(ux, ux, fmaf(uy, uy, kp1 * uz * uz));
+      const float B = 2.f * (c * fmaf(oxf, ux, fmaf(oyf, uy, kp1 * ozf * uz)) - uz);
+      const float C = fmaf(c, fmaf(oxf, oxf, fmaf(oyf, oyf, kp1 * ozf * ozf)),
+                           -2.f * ozf);
+      const float disc = fmaf(B, B, -4.f * A * C);
+      const bool real = disc >= 0.f;
+      const float sq = sqrtf(real ? disc : 0.f);
+      float ta, tb;  // roots with -sqrt and +sqrt
+      if (fabsf(A) < 1e-12f) {
+        ta = -C / B;
+        tb = ta;
+      } else {
+        const float qq = -0.5f * (B + copysignf(sq, B));
+        const float r1 = qq / A, r2 = C / qq;
+        if (B >= 0.f) {
+          ta = r1;
+          tb = r2;
+        } else {
+          ta = r2;
+          tb = r1;
+        }
+      }
+      // vertex-sheet test z (c r^2 - z) >= 0 on each candidate
+      const float za = fmaf(ta, uz, ozf), xa = fmaf(ta, ux, oxf), ya = fmaf(ta, uy, oyf);
+      const float zb = fmaf(tb, uz, ozf), xb = fmaf(tb, ux, oxf), yb = fmaf(tb, uy, oyf);
+      const bool va = real && (za * (c * fmaf(xa, xa, ya * ya) - za) >= 0.f);
+      const bool vb = real && (zb * (c * fmaf(xb, xb, yb * yb) - zb) >= 0.f);
+      ta = va ? ta : INFINITY;
+      tb = vb ? tb : INFINITY;
+      t = (fabsf(ta) <= fabsf(tb)) ? ta : tb;
+      break;
+    }
+    case OTX_SAG_PARABOLA: {
+      const float f = s.sag_focal_length;
+      const float a = fmaf(ux, ux, uy * uy);
+      // a t^2 + 2 hb t + cc = 0
+      const float hb = fmaf(oxf, ux, oyf * uy) - 2.f * f * uz;
+      const float cc = fmaf(oxf, oxf, oyf * oyf) - 4.f * f * ozf;
+      if (a > 1e-10f) {
+        const float sq = sqrtf(fmaf(hb, hb, -a * cc));
+        const float sg = sgnf(f * uz);
+        if (sg != 0.f && sgnf(-hb) == sg)
+          t = cc / (-hb + sg * sq);
+        else
+          t = (-hb - sg * sq) / a;
+      } else {
+        t = cc / (4.f * f * uz);
+      }
+      break;
+    }
+    default:  // toroid: start from the vertex plane
+      t = -ozf / uz;
+      break;
+  }
+  // point on the ray, small coordinates: (o_hi + t u) + o_lo
+  x = fmaf(t, ux, ox) + lo[0];
+  y = fmaf(t, uy, oy) + lo[1];
+  z = fmaf(t, uz, oz) + lo[2];
+  if (s.sag_type == OTX_SAG_TOROID) {
+    const int iters = newton_max > 0 ? newton_max : 12;
+    bool conv = false;
+    for (int i = 0; i < iters; ++i) {
+      const float dt = newton_step(s, x, y, z, ux, uy, uz);
+      t -= dt;
+      if (fabsf(dt) <= 1e-7f * (1.f + fabsf(t))) {
+        conv = true;
+        break;
+      }
+    }
+    if (!conv) {
+      x = y = z = NAN;
+    }
+  } else if (isfinite(t)) {
+    t -= newton_step(s, x, y, z, ux, uy, uz);
+  }
+  return t;
+}
+
+// Surface normal at a point of the sag (z < 0 convention).
+//   flat     optika/sags/_flat.py:41-45
+//   sphere   optika/sags/_spherical.py:125-146
+//   conic    optika/sags/_conic.py:50-75
+//   parabola optika/sags/_parabolic.py:40-63 (equal to the k = -1 conic)
+//   toroid   optika/sags/_toroidal.py:59-88
+__device__ __forceinline__ void normal(const otx_surface& s, float x, float y,
+                                       float& nx, float& ny, float& nz) {
+  switch (s.sag_type) {
+    case OTX_SAG_SPHERE: {
+      const float c = s.sag_curvature;
+      nx = c * x;
+      ny = c * y;
+      nz = -sqrtf(1.f - nx * nx - ny * ny);
+      return;
+    }
+    case OTX_SAG_CONIC:
+    case OTX_SAG_PARABOLA:
+    case OTX_SAG_TOROID: {
+      float gx, gy;
+      sag_eval(s, x, y, gx, gy);
+      const float inv = rsqrtf(fmaf(gx, gx, fmaf(gy, gy, 1.f)));
+      nx = gx * inv;
+      ny = gy * inv;
+      nz = -inv;
+      return;
+    }
+    default:
+      nx = 0.f;
+      ny = 0.f;
+      nz = -1.f;
+      return;
+  }
+}
+
+// ---------------------------------------------------------------- Snell
+
+// Vector Snell's law, optika/materials/_snells_law.py:341-366:
+//   d = -a.u + sgn (2 m - 1) sqrt(1/r^2 + (a.u)^2 - |a|^2),  b = r (a + d u)
+// with sgn = -copysign(1, a.u).  The radicand's (1/r^2 - |a|^2) is formed
+// as ((n2/n1)^2 - 1) - (|a|^2 - 1) with fused multiply-adds so that unit
+// directions reflect without the 1 - |a|^2 rounding of a plain FP32 sum;
+// equal indices (mirrors, vacuum to vacuum) skip the divisions (r = 1).
+__device__ __forceinline__ void snell(float& ax, float& ay, float& az, float n1,
+                                      float n2, bool mirror, float ux,
+                                      float uy, float uz) {
+  float e = fmaf(ax, ax, -1.f);
+  e = fmaf(ay, ay, e);
+  e = fmaf(az, az, e);
+  const float au = fmaf(ax, ux, fmaf(ay, uy, az * uz));
+  const float sgn = -copysignf(1.f, au);
+  float r = 1.f, q2m1 = 0.f;
+  if (n1 != n2) {
+    r = n1 / n2;
+    const float q = n2 / n1;
+    q2m1 = (q - 1.f) * (q + 1.f);
+  }
+  const float rad = fmaf(au, au, q2m1 - e);
+  const float d = -au + sgn * (mirror ? 1.f : -1.f) * sqrtf(rad);
+  ax = r * fmaf(d, ux, ax);
+  ay = r * fmaf(d, uy, ay);
+  az = r * fmaf(d, uz, az);
+}
+
+// ---------------------------------------------------------------- rulings
+
+// Spacing vector kappa (length d, along the ruling-plane normal).
+//   constant     optika/rulings/_spacing.py:69-74
+//   polynomial   optika/rulings/_spacing.py:109-128
+//   holographic  optika/rulings/_spacing.py:295-328
+__device__ __forceinline__ void ruling_kappa(const otx_surface& s, float x,
+                                             float y, float z, float nx,
+                                             float ny, float nz, float& kx,
+                                             float& ky, float& kz) {
+  switch (s.rule_type) {
+    case OTX_RULE_CONSTANT: {
+      const float d = s.rule_coef[0];
+      kx = d * s.rule_normal[0];
+      ky = d * s.rule_normal[1];
+      kz = d * s.rule_normal[2];
+      return;
+    }
+    case OTX_RULE_POLY1D: {
+      float px = x, py = y, pz = z;
+      affine_point_folded(s.rule_xform, px, py, pz);
+      const float xs = fmaf(px, s.rule_normal[0],
+                            fmaf(py, s.rule_normal[1], pz * s.rule_normal[2]));
+      float d = 0.f;  // Horner over the dense coefficient table
+      for (int k = s.rule_num_terms - 1; k >= 0; --k) d = fmaf(d, xs, s.rule_coef[k]);
+      kx = d * s.rule_normal[0];
+      ky = d * s.rule_normal[1];
+      kz = d * s.rule_normal[2];
+      return;
+    }
+    case OTX_RULE_HOLOGRAPHIC: {
+      float r1x = x - s.holo_x1[0], r1y = y - s.holo_x1[1], r1z = z - s.holo_x1[2];
+      float r2x = x - s.holo_x2[0], r2y = y - s.holo_x2[1], r2z = z - s.holo_x2[2];
+      const float i1 = s.holo_d1 * rsqrtf(r1x * r1x + r1y * r1y + r1z * r1z);
+      const float i2 = s.holo_d2 * rsqrtf(r2x * r2x + r2y * r2y + r2z * r2z);
+      const float drx = r1x * i1 - r2x * i2;
+      const float dry = r1y * i1 - r2y * i2;
+      const float drz = r1z * i1 - r2z * i2;
+      // aq = n x dr ; a = |aq| ; q = aq / a ; d = lambda / a ; kappa = d q x n
+      const float aqx = ny * drz - nz * dry;
+      const float aqy = nz * drx - nx * drz;
+      const float aqz = nx * dry - ny * drx;
+      const float a2 = aqx * aqx + aqy * aqy + aqz * aqz;
+      const float sc = s.holo_wavelength / a2;  // (lambda / a) / a
+      kx = sc * (aqy * nz - aqz * ny);
+      ky = sc * (aqz * nx - aqx * nz);
+      kz = sc * (aqx * ny - aqy * nx);
+      return;
+    }
+    default:
+      kx = ky = kz = 0.f;
+      return;
+  }
+}
+
+// Effective incident direction, optika/rulings/_rulings.py:124-126:
+//   a + sign(a.n) m lambda g / (n d),  g = kappa / d.
+__device__ __forceinline__ void incident_effective(const otx_surface& s,
+                                                   Ray& r, float nx, float ny,
+                                                   float nz) {
+  float kx, ky, kz;
+  ruling_kappa(s, r.px, r.py, r.pz, nx, ny, nz, kx, ky, kz);
+  const float d2 = kx * kx + ky * ky + kz * kz;
+  const float an = r.dx * nx + r.dy * ny + r.dz * nz;
+  const float w_mm = r.wl * 1e-6f;
+  const float f = sgnf(an) * s.rule_order * w_mm / (r.n * d2);
+  r.dx = fmaf(f, kx, r.dx);
+  r.dy = fmaf(f, ky, r.dy);
+  r.dz = fmaf(f, kz, r.dz);
+}
+
+// ---------------------------------------------------------------- apertures
+
+// optika/apertures/_apertures.py: circular :292-314, sector :438-480,
+// elliptical :640-663, polygonal :739-778, rectangular :941-968.
+// Comparisons are inclusive (<=) as in the reference; NaN coordinates test
+// false before inversion.
+__device__ __forceinline__ bool aperture_inside(const otx_system& sys,
+                                                const otx_surface& s, float x,
+                                                float y, float z) {
+  const int flags = s.aper_flags;
+  if (!(flags & OTX_APER_FLAG_ACTIVE)) return true;
+  if (flags & OTX_APER_FLAG_TRANSFORM) affine_point_folded(s.aper_to_local, x, y, z);
+  bool m;
+  switch (s.aper_type) {
+    case OTX_APER_CIRCULAR:
+      m = sqrtf(fmaf(x, x, y * y)) <= s.aper_p[0];
+      break;
+    case OTX_APER_RECTANGULAR:
+      m = (-s.aper_p[0] <= x) && (x <= s.aper_p[0]) && (-s.aper_p[1] <= y) &&
+          (y <= s.aper_p[1]);
+      break;
+    case OTX_APER_ELLIPTICAL: {
+      const float a = x / s.aper_p[0], b = y / s.aper_p[1];
+      m = (a * a + b * b) <= 1.f;
+      break;
+    }
+    case OTX_APER_SECTOR: {
+      const bool mr = sqrtf(fmaf(x, x, y * y)) <= s.aper_p[0];
+      const float ang = atan2f(y, x);
+      const float twopi = 6.283185307179586f;
+      const float ap = (ang < 0.f) ? ang + twopi : ang;
+      const float an = (ang > 0.f) ? ang - twopi : ang;
+      const float a0 = s.aper_p[1], a1 = s.aper_p[2];
+      const bool ma = ((a0 < ap) && (ap < a1)) || ((a0 < an) && (an < a1));
+      m = mr && ma;
+      break;
+    }
+    case OTX_APER_POLYGON: {
+      // even-odd crossing test over the vertex loop
+      bool inside = false;
+      const int b = s.aper_vertex_begin, cnt = s.aper_vertex_count;
+      for (int i = 0, j = cnt - 1; i < cnt; j = i++) {
+        const float xi = sys.vertices[2 * (b + i)], yi = sys.vertices[2 * (b + i) + 1];
+        const float xj = sys.vertices[2 * (b + j)], yj = sys.vertices[2 * (b + j) + 1];
+        if (((yi > y) != (yj > y)) && (x < (xj - xi) * (y - yi) / (yj - yi) + xi))
+          inside = !inside;
+      }
+      m = inside;
+      break;
+    }
+    default:
+      m = true;
+      break;
+  }
+  if (flags & OTX_APER_FLAG_INVERTED) m = !m;
+  return m;
+}
+
+// ---------------------------------------------------------------- complex
+
+struct cf {
+  float re, im;
+};
+__device__ __forceinline__ cf cadd(cf a, cf b) { return cf{a.re + b.re, a.im + b.im}; }
+__device__ __forceinline__ cf csub(cf a, cf b) { return cf{a.re - b.re, a.im - b.im}; }
+__device__ __forceinline__ cf cmul(cf a, cf b) {
+  return cf{fmaf(a.re, b.re, -a.im * b.im), fmaf(a.re, b.im, a.im * b.re)};
+}
+__device__ __forceinline__ cf cscale(cf a, float s) { return cf{a.re * s, a.im * s}; }
+__device__ __forceinline__ cf cconj(cf a) { return cf{a.re, -a.im}; }
+__device__ __forceinline__ float cabs2(cf a) { return fmaf(a.re, a.re, a.im * a.im); }
+// a / b for b of moderate magnitude (indices, cosines): conj(b) / |b|^2.
+__device__ __forceinline__ cf cdiv(cf a, cf b) {
+  return cscale(cmul(a, cconj(b)), 1.f / cabs2(b));
+}
+// Principal square root (branch cut on the negative real axis, as numpy),
+// for arguments of moderate magnitude.
+__device__ __forceinline__ cf csqrt(cf z) {
+  const float m = sqrtf(cabs2(z));
+  const float h = 0.5f * (m + fabsf(z.re));
+  if (h == 0.f) return cf{0.f, z.im};
+  const float rs = rsqrtf(h);
+  const float t = h * rs;                   // sqrt(h)
+  const float u = 0.5f * fabsf(z.im) * rs;  // |im| / (2 sqrt(h))
+  if (z.re >= 0.f) return cf{t, copysignf(u, z.im)};
+  return cf{u, copysignf(t, z.im)};
+}
+
+struct cm2 {
+  cf a, b, c, d;  // [[a, b], [c, d]]
+};
+__device__ __forceinline__ cm2 cm_mul(const cm2& x, const cm2& y) {
+  return cm2{cadd(cmul(x.a, y.a), cmul(x.b, y.c)), cadd(cmul(x.a, y.b), cmul(x.b, y.d)),
+             cadd(cmul(x.c, y.a), cmul(x.d, y.c)), cadd(cmul(x.c, y.b), cmul(x.d, y.d))};
+}
+
+// Exact power-of-two rescaling of a transfer matrix so that its largest
+// component is O(1); the exponent is accumulated separately.
+__device__ __forceinline__ void cm_normalize(cm2& m, int& exp2) {
+  const float mx = fmaxf(fmaxf(fmaxf(fabsf(m.a.re), fabsf(m.a.im)),
+                               fmaxf(fabsf(m.b.re), fabsf(m.b.im))),
+                         fmaxf(fmaxf(fabsf(m.c.re), fabsf(m.c.im)),
+                               fmaxf(fabsf(m.d.re), fabsf(m.d.im))));
+  if (!(mx > 0.f) || !isfinite(mx)) return;
+  const int e = ilogbf(mx);
+  const float s = ldexpf(1.f, -e);
+  m.a = cscale(m.a, s);
+  m.b = cscale(m.b, s);
+  m.c = cscale(m.c, s);
+  m.d = cscale(m.d, s);
+  exp2 += e;
+}
+
+// Complex index of a layer at a vacuum wavelength (nm).
+__device__ __forceinline__ cf layer_n(const otx_system& sys, const otx_layer& L,
+                                      float wl) {
+  if (L.table < 0) return cf{L.n_re, L.n_im};
+  const otx_table T = sys.tables[L.table];
+  const float* base = reinterpret_cast<const float*>(sys.table_data) + T.offset;
+  const float* xs = base;
+  const float* ns = base + T.count;
+  const float* ks = base + 2 * T.count;
+  const int cnt = T.count;
+  if (!(wl > xs[0])) return cf{ns[0], ks[0]};
+  if (!(wl < xs[cnt - 1])) return cf{ns[cnt - 1], ks[cnt - 1]};
+  int lo = 0, hi = cnt - 1;  // xs[lo] < wl < xs[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (xs[mid] <= wl)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  const float w = (wl - xs[lo]) / (xs[hi] - xs[lo]);
+  return cf{fmaf(w, ns[hi] - ns[lo], ns[lo]), fmaf(w, ks[hi] - ks[lo], ks[lo])};
+}
+
+// Running state of the transfer-matrix product for one polarisation.
+//
+// The reference's refraction matrix W = [[1, r], [r, 1]] / t
+// (optika/materials/matrices.py:127-161) equals W' / (2 q_i) with
+// W' = [[q_i + q_j, q_i - q_j], [q_i - q_j, q_i + q_j]].  The state keeps
+// the product of the W' (times the propagation matrices U) and, when
+// transmission is wanted, the product of |2 q_i|^2 separately:
+// r = M21 / M11 is unchanged and |t|^2 = prod |2 q_i|^2 / |M'11|^2, so no
+// complex division is needed.  Both products carry power-of-two exponents.
+// q is n cos for s and conj(cos) / n = conj(n cos) / |n|^2 for p.
+struct MLState {
+  cm2 m;      // unnormalised product
+  int e;      // its exponent
+  bool first; // product still the identity
+  float t;    // prod |2 q_i|^2 mantissa
+  int te;     // and its exponent
+  cf q;       // q of the current medium
+  cf inv0;    // (n0 sin0)^2, Snell invariant
+  bool where;
+};
+
+// q of the medium of index nj, from the Snell invariant:
+// cos_j = sqrt(1 - (n0 sin0)^2 / n_j^2) equals the reference's chained
+// optika/materials/_snells_law.py:13-38.
+__device__ __forceinline__ cf medium_q(const cf& inv0, const cf& nj, bool pol_p) {
+  const cf nj2 = cmul(nj, nj);
+  const cf ratio = cscale(cmul(inv0, cconj(nj2)), 1.f / cabs2(nj2));
+  const cf cj = csqrt(cf{1.f - ratio.re, -ratio.im});
+  const cf w = cmul(nj, cj);
+  return pol_p ? cscale(cconj(w), 1.f / cabs2(nj)) : w;
+}
+
+__device__ __forceinline__ void ml_times(MLState& st, const cm2& t, int te) {
+  if (st.first) {
+    st.m = t;
+    st.e = te;
+    st.first = false;
+  } else {
+    st.m = cm_mul(st.m, t);
+    st.e += te;
+  }
+  cm_normalize(st.m, st.e);
+}
+
+// Multiply the running product by one layer's W' (and its propagation U),
+// optika/materials/_layers.py:229-277; thickness 0 is the substrate.
+template <bool NEED_T>
+__device__ __forceinline__ void layer_step(MLState& st, cf nj, float thickness, float wl,
+                                           bool pol_p) {
+  const cf qj = medium_q(st.inv0, nj, pol_p);
+  const cf a = cadd(st.q, qj), b = csub(st.q, qj);
+  // U = diag(exp(-i beta), exp(i beta)), beta = 2 pi h n cos / lambda
+  bool wprop = true;
+  cm2 tm = cm2{a, b, b, a};
+  if (thickness != 0.f) {
+    const cf ncos = pol_p ? cscale(cconj(qj), cabs2(nj)) : qj;  // n cos
+    const cf beta = cscale(ncos, 6.283185307179586f * thickness / wl);
+    float sn, cs;
+    sincosf(beta.re, &sn, &cs);
+    const float g = expf(beta.im);  // |exp(-i beta)|
+    wprop = g < 1e10f;
+    if (wprop) {
+      const cf em{g * cs, -g * sn};
+      const float gi = 1.f / g;
+      const cf ep{gi * cs, gi * sn};
+      tm = cm2{cmul(a, em), cmul(b, ep), cmul(b, em), cmul(a, ep)};
+    }
+  }
+  if (st.where) {
+    ml_times(st, tm, 0);
+    if (NEED_T) {
+      int e;
+      st.t = frexpf(st.t * 4.f * cabs2(st.q), &e);
+      st.te += e;
+    }
+  }
+  st.where = st.where && wprop;
+  st.q = qj;
+}
+
+__device__ __forceinline__ void cm_pow(cm2 base, int bexp, int e, cm2& acc, int& aexp) {
+  bool first = true;
+  while (e > 0) {
+    if (e & 1) {
+      if (first) {
+        acc = base;
+        aexp = bexp;
+        first = false;
+      } else {
+        acc = cm_mul(acc, base);
+        aexp += bexp;
+        cm_normalize(acc, aexp);
+      }
+    }
+    e >>= 1;
+    if (e) {
+      base = cm_mul(base, base);
+      bexp *= 2;
+      cm_normalize(base, bexp);
+    }
+  }
+}
+
+template <bool NEED_T>
+__device__ __forceinline__ void run_layers(MLState& st, const otx_system& sys, int begin,
+                                           int count, float wl, bool pol_p) {
+  for (int i = 0; i < count; ++i) {
+    const otx_layer& L = sys.layers[begin + i];
+    layer_step<NEED_T>(st, layer_n(sys, L, wl), L.thickness, wl, pol_p);
+  }
+}
+
+// Reflectivity and transmissivity of one polarisation of a stack,
+// optika/materials/_multilayers.py:187-237 (coefficients) and :485-532
+// (R = |r|^2, T = |t|^2 Re(q_sub / q_amb)).  A periodic block is its first
+// period times the period matrix to the power num_periods - 1
+// (optika/materials/_layers.py:611-645), by repeated squaring.
+template <bool NEED_T>
+__device__ __forceinline__ void multilayer_pol(const otx_system& sys, const otx_stack& K,
+                                               float wl, float cos0, cf n0, bool pol_p,
+                                               float& R, float& T) {
+  MLState st;
+  st.e = 0;
+  st.first = true;
+  st.t = 1.f;
+  st.te = 0;
+  st.inv0 = cscale(cmul(n0, n0), fmaf(-cos0, cos0, 1.f));
+  st.q = pol_p ? cscale(cconj(n0), cos0 / cabs2(n0)) : cscale(n0, cos0);
+  const cf q0 = st.q;
+  st.where = true;
+  run_layers<NEED_T>(st, sys, K.pre_begin, K.pre_count, wl, pol_p);
+  if (K.per_count > 0 && K.num_periods > 0) {
+    // first period from the current medium
+    run_layers<NEED_T>(st, sys, K.per_begin, K.per_count, wl, pol_p);
+    // one period from the period's own last medium, to num_periods - 1
+    MLState per = st;
+    per.first = true;
+    per.e = 0;
+    per.t = 1.f;
+    per.te = 0;
+    run_layers<NEED_T>(per, sys, K.per_begin, K.per_count, wl, pol_p);
+    const int reps = K.num_periods - 1;
+    if (!per.first && reps > 0) {
+      cm2 pm;
+      int pe = 0;
+      cm_pow(per.m, per.e, reps, pm, pe);
+      ml_times(st, pm, pe);
+      if (NEED_T) {
+        for (int i = 0; i < reps; ++i) {
+          int e;
+          st.t = frexpf(st.t * per.t, &e);
+          st.te += per.te + e;
+        }
+      }
+    }
+    st.where = per.where;
+    st.q = per.q;
+  }
+  run_layers<NEED_T>(st, sys, K.post_begin, K.post_count, wl, pol_p);
+  cf nsub{1.f, 0.f};
+  if (K.substrate >= 0) nsub = layer_n(sys, sys.layers[K.substrate], wl);
+  layer_step<NEED_T>(st, nsub, 0.f, wl, pol_p);
+  // R = |M21|^2 / |M11|^2 (exponents cancel)
+  const float m11 = cabs2(st.m.a);
+  R = cabs2(st.m.c) / m11;
+  T = 0.f;
+  if (NEED_T && st.where) {
+    // |t|^2 = prod |2q|^2 / |M'11|^2 ; T = |t|^2 Re(q_sub / q_amb)
+    T = ldexpf(st.t / m11, st.te - 2 * st.e) * cdiv(st.q, q0).re;
+  }
+}
+
+// Both polarisations, for the standalone multilayer kernel.
+__device__ __forceinline__ void multilayer(const otx_system& sys, const otx_stack& K,
+                                           float wl, float cos0, cf n0, float& Rs,
+                                           float& Rp, float& Ts, float& Tp) {
+  multilayer_pol<true>(sys, K, wl, cos0, n0, false, Rs, Ts);
+  multilayer_pol<true>(sys, K, wl, cos0, n0, true, Rp, Tp);
+}
+
+__device__ __forceinline__ bool stack_has_layers(const otx_stack& K) {
+  return K.pre_count > 0 || (K.per_count > 0 && K.num_periods > 0) || K.post_count > 0;
+}
+
+// Substrate-only stack (a bare coating, or a film of no layers): the
+// multilayer product reduces to one interface, r = (q0 - q1) / (q0 + q1),
+// t = 2 q0 / (q0 + q1); returns the s/p average of R (mirror) or T.
+__device__ __forceinline__ float fresnel_efficiency(const otx_system& sys, const otx_stack& K,
+                                                    bool mirror, float wl, float cos0, cf n0) {
+  cf n1{1.f, 0.f};
+  if (K.substrate >= 0) n1 = layer_n(sys, sys.layers[K.substrate], wl);
+  const cf inv0 = cscale(cmul(n0, n0), fmaf(-cos0, cos0, 1.f));
+  float acc = 0.f;
+#pragma unroll
+  for (int p = 0; p < 2; ++p) {
+    const bool pol_p = p == 1;
+    const cf q0 = pol_p ? cscale(cconj(n0), cos0 / cabs2(n0)) : cscale(n0, cos0);
+    const cf q1 = medium_q(inv0, n1, pol_p);
+    const float den = cabs2(cadd(q0, q1));
+    if (mirror) {
+      acc += cabs2(csub(q0, q1)) / den;
+    } else {
+      acc += 4.f * cabs2(q0) / den * cdiv(q1, q0).re;
+    }
+  }
+  return 0.5f * acc;
+}
+
+// Out-of-line efficiency of a layered stack for the trace kernel (systems
+// without layered coatings never call it): the s/p average of R or T.
+static __device__ __noinline__ float multilayer_efficiency_call(const otx_system& sys,
+                                                                int stack, bool mirror,
+                                                                float wl, float cos0,
+                                                                float n_re, float n_im) {
+  const otx_stack& K = sys.stacks[stack];
+  float acc = 0.f;
+  for (int p = 0; p < 2; ++p) {
+    float R, T;
+    if (mirror) {
+      multilayer_pol<false>(sys, K, wl, cos0, cf{n_re, n_im}, p == 1, R, T);
+      acc += R;
+    } else {
+      multilayer_pol<true>(sys, K, wl, cos0, cf{n_re, n_im}, p == 1, R, T);
+      acc += T;
+    }
+  }
+  return 0.5f * acc;
+}
+
+// ---------------------------------------------------------------- surface
+
+// One surface of optika/surfaces.py:123-198 for a ray already expressed in
+// the previous frame.  Returns with the ray in this surface's frame.  ML
+// selects the kernel variant that can evaluate layered multilayer stacks
+// (chosen by the host when the system has one).
+template <bool ML>
+__device__ __forceinline__ void propagate_surface(const otx_system& sys,
+                                                  const otx_surface& s,
+                                                  Ray& r) {
+  // transformation.inverse (surfaces.py:141-142), float-float translation
+  float lo[3];
+  float ox = r.px, oy = r.py, oz = r.pz;
+  affine_point(s.to_local, ox, oy, oz, lo);
+  rotate(s.to_local, r.dx, r.dy, r.dz);
+
+  // sag.propagate_rays (sags/_abc.py:109-122)
+  float x, y, z;
+  const float t = intercept(s, sys.newton_iterations, ox, oy, oz, lo, r.dx,
+                            r.dy, r.dz, x, y, z);
+  r.px = x;
+  r.py = y;
+  r.pz = z;
+  if (r.att != 0.f) {
+    const float len = fabsf(t) * sqrtf(r.dx * r.dx + r.dy * r.dy + r.dz * r.dz);
+    r.inten *= expf(-r.att * len);
+  }
+  opl_add(r, r.n, t);
+
+  float nx, ny, nz;
+  normal(s, x, y, nx, ny, nz);
+
+  if (s.rule_type != OTX_RULE_NONE) incident_effective(s, r, nx, ny, nz);
+
+  // material (surfaces.py:160-181)
+  const float n1 = r.n;
+  float n2 = n1;
+  float att2 = r.att;
+  float eff = 1.f;
+  bool mirror = false;
+  switch (s.mat_type) {
+    case OTX_MAT_VACUUM:
+      n2 = 1.f;
+      att2 = 0.f;
+      break;
+    case OTX_MAT_MIRROR:
+      mirror = true;
+      break;
+    case OTX_MAT_GLASS: {
+      // Sellmeier, optika/materials/_materials.py:428-438
+      const float w2 = r.wl * r.wl;
+      float s2 = 1.f;
+      for (int i = 0; i < 3; ++i) s2 += s.sellmeier_b[i] * w2 / (w2 - s.sellmeier_c[i]);
+      n2 = sqrtf(s2);
+      att2 = 0.f;
+      break;
+    }
+    case OTX_MAT_MULTILAYER_MIRROR:
+    case OTX_MAT_MULTILAYER_FILM: {
+      mirror = (s.mat_type == OTX_MAT_MULTILAYER_MIRROR);
+      // n = n_ray + i att lambda / (4 pi), cos = -a.n (_multilayers.py:924-932)
+      const float k = r.att * (r.wl * 1e-6f) * 0.07957747154594767f;
+      const float cos0 = -(r.dx * nx + r.dy * ny + r.dz * nz);
+      const otx_stack& K = sys.stacks[s.mat_stack];
+      if (ML && stack_has_layers(K))
+        eff = multilayer_efficiency_call(sys, s.mat_stack, mirror, r.wl, cos0, n1, k);
+      else
+        eff = fresnel_efficiency(sys, K, mirror, r.wl, cos0, cf{n1, k});
+      break;
+    }
+    default:
+      break;
+  }
+  if (s.rule_type != OTX_RULE_NONE) eff *= s.rule_efficiency;
+  // wavelength_2 = wavelength_1 / (n1 / n2)   (surfaces.py:162-165)
+  if (n2 != n1) r.wl = r.wl / (n1 / n2);
+  snell(r.dx, r.dy, r.dz, n1, n2, mirror, nx, ny, nz);
+  r.inten *= eff;
+  r.att = att2;
+  r.n = n2;
+
+  // aperture.clip_rays (apertures/_apertures.py:82-102)
+  if (s.aper_type != OTX_APER_NONE) {
+    const bool on_dir = (s.aper_flags & OTX_APER_FLAG_DIRECTION) != 0;
+    const bool m = on_dir ? aperture_inside(sys, s, r.dx, r.dy, r.dz)
+                          : aperture_inside(sys, s, r.px, r.py, r.pz);
+    r.ok = r.ok && m;
+  }
+}
+
+}  // namespace otx

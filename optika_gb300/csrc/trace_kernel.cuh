@@ -1,0 +1,202 @@
+// Fused trace kernel template, instantiated per input mode in
+// trace_rays.cu, trace_grid_inf.cu and trace_grid_fin.cu so that the modes
+// compile in parallel.
+#pragma once
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "../../include/optika_gb300.h"
+#include "trace_device.cuh"
+#include "trace_kernel_decl.h"
+
+namespace otx {
+
+
+// direction cosines from (azimuth, elevation), optika/_util.py:69-73
+__device__ __forceinline__ void direction_from_angles(float ax, float ay,
+                                                      float& dx, float& dy,
+                                                      float& dz) {
+  float sx, cx, sy, cy;
+  sincosf(ax, &sx, &cx);
+  sincosf(ay, &sy, &cy);
+  dx = -cy * sx;
+  dy = -sy;
+  dz = cy * cx;
+}
+
+template <int MODE>
+__device__ __forceinline__ void load_ray(const TraceArgs& a, int64_t i, Ray& r) {
+  if (MODE == OTX_INPUT_RAYS) {
+    const otx_rays& in = a.in;
+    r.px = reinterpret_cast<const float*>(in.px)[i];
+    r.py = reinterpret_cast<const float*>(in.py)[i];
+    r.pz = reinterpret_cast<const float*>(in.pz)[i];
+    r.dx = reinterpret_cast<const float*>(in.dx)[i];
+    r.dy = reinterpret_cast<const float*>(in.dy)[i];
+    r.dz = reinterpret_cast<const float*>(in.dz)[i];
+    r.wl = in.wavelength ? reinterpret_cast<const float*>(in.wavelength)[i] : 0.f;
+    r.inten = in.intensity ? reinterpret_cast<const float*>(in.intensity)[i] : 1.f;
+    r.att = in.attenuation ? reinterpret_cast<const float*>(in.attenuation)[i] : 0.f;
+    r.n = in.index_refraction ? reinterpret_cast<const float*>(in.index_refraction)[i] : 1.f;
+    r.ok = in.unvignetted ? (reinterpret_cast<const uint8_t*>(in.unvignetted)[i] != 0) : true;
+    const double o = in.opl ? reinterpret_cast<const double*>(in.opl)[i] : 0.0;
+    r.opl_hi = (float)o;
+    r.opl_lo = (float)(o - (double)r.opl_hi);
+  } else {
+    const otx_grid& g = a.grid;
+    const float wl = reinterpret_cast<const float*>(g.wavelength)[i * g.stride_wavelength];
+    const float fx = reinterpret_cast<const float*>(g.field_x)[i * g.stride_field];
+    const float fy = reinterpret_cast<const float*>(g.field_y)[i * g.stride_field];
+    const float qx = reinterpret_cast<const float*>(g.pupil_x)[i * g.stride_pupil];
+    const float qy = reinterpret_cast<const float*>(g.pupil_y)[i * g.stride_pupil];
+    if (MODE == OTX_INPUT_GRID_INFINITY) {
+      r.px = qx;
+      r.py = qy;
+      direction_from_angles(fx, fy, r.dx, r.dy, r.dz);
+    } else {
+      r.px = fx;
+      r.py = fy;
+      direction_from_angles(qx, qy, r.dx, r.dy, r.dz);
+    }
+    r.pz = 0.f;
+    r.wl = wl;
+    r.inten = g.intensity ? reinterpret_cast<const float*>(g.intensity)[i * g.stride_intensity] : 1.f;
+    r.att = 0.f;
+    r.n = 1.f;
+    r.ok = true;
+    r.opl_hi = 0.f;
+    r.opl_lo = 0.f;
+  }
+}
+
+template <bool IDENTITY>
+__device__ __forceinline__ void store_ray(const otx_rays& o, int64_t i,
+                                          const otx_affine& f, const Ray& r) {
+  float x = r.px, y = r.py, z = r.pz;
+  float dx = r.dx, dy = r.dy, dz = r.dz;
+  if (!IDENTITY) {
+    affine_point_folded(f, x, y, z);
+    rotate(f, dx, dy, dz);
+  }
+  if (o.px) reinterpret_cast<float*>(o.px)[i] = x;
+  if (o.py) reinterpret_cast<float*>(o.py)[i] = y;
+  if (o.pz) reinterpret_cast<float*>(o.pz)[i] = z;
+  if (o.dx) reinterpret_cast<float*>(o.dx)[i] = dx;
+  if (o.dy) reinterpret_cast<float*>(o.dy)[i] = dy;
+  if (o.dz) reinterpret_cast<float*>(o.dz)[i] = dz;
+  if (o.wavelength) reinterpret_cast<float*>(o.wavelength)[i] = r.wl;
+  if (o.intensity) reinterpret_cast<float*>(o.intensity)[i] = r.inten;
+  if (o.attenuation) reinterpret_cast<float*>(o.attenuation)[i] = r.att;
+  if (o.index_refraction) reinterpret_cast<float*>(o.index_refraction)[i] = r.n;
+  if (o.unvignetted) reinterpret_cast<uint8_t*>(o.unvignetted)[i] = r.ok ? 1 : 0;
+  if (o.opl) reinterpret_cast<double*>(o.opl)[i] = (double)r.opl_hi + (double)r.opl_lo;
+}
+
+// Histogram bin of a ray in the sensor frame, numpy.histogramdd edges:
+// [e_j, e_j+1) with the last edge inclusive; outside and NaN are dropped
+// (optika/sensors/_sensors.py:141-155).
+__device__ __forceinline__ int64_t sensor_bin(const otx_sensor& S, const Ray& r) {
+  const float hx = S.lo_x + S.num_x * S.width_x;
+  const float hy = S.lo_y + S.num_y * S.width_y;
+  if (!(r.px >= S.lo_x && r.px <= hx && r.py >= S.lo_y && r.py <= hy)) return -1;
+  int ix = (int)floorf((r.px - S.lo_x) * S.inv_width_x);
+  int iy = (int)floorf((r.py - S.lo_y) * S.inv_width_y);
+  ix = min(max(ix, 0), S.num_x - 1);
+  iy = min(max(iy, 0), S.num_y - 1);
+  int iw = 0;
+  if (S.w_hi > S.w_lo) {
+    if (!(r.wl >= S.w_lo && r.wl <= S.w_hi)) return -1;
+    iw = (int)floorf((r.wl - S.w_lo) * S.inv_width_w);
+    iw = min(max(iw, 0), S.num_w - 1);
+  }
+  return ((int64_t)iw * S.num_x + ix) * S.num_y + iy;
+}
+
+__device__ __forceinline__ void bin_ray(const otx_sensor& S, const otx_image& img,
+                                        const Ray& r) {
+  if (!r.ok) return;
+  const int64_t b = sensor_bin(S, r);
+  if (b < 0) return;
+  if (img.counts) atomicAdd(reinterpret_cast<unsigned int*>(img.counts) + b, 1u);
+  if (img.flux) atomicAdd(reinterpret_cast<float*>(img.flux) + b, r.inten);
+}
+
+// Minimum resident CTAs per SM requested from the register allocator
+// (256 threads each).
+#ifndef OTX_TRACE_MIN_BLOCKS
+#define OTX_TRACE_MIN_BLOCKS 1
+#endif
+
+template <int RPT, int MODE, bool ACC, bool ML>
+__global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
+    k_trace(const __grid_constant__ otx_system sys,
+            const __grid_constant__ TraceArgs a) {
+  const int64_t n = a.count;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x * RPT;
+  const int ns = sys.num_surfaces;
+  const bool bin = (a.img.counts != 0) || (a.img.flux != 0);
+  const bool final_identity = (sys.flags & OTX_SYS_FLAG_FINAL_IDENTITY) != 0;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x * RPT + threadIdx.x; base < n;
+       base += step) {
+    Ray r[RPT];
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int64_t i = base + (int64_t)k * blockDim.x;
+      if (i < n) load_ray<MODE>(a, i, r[k]);
+    }
+    for (int s = 0; s < ns; ++s) {
+      const otx_surface& S = sys.surfaces[s];
+#pragma unroll
+      for (int k = 0; k < RPT; ++k) {
+        const int64_t i = base + (int64_t)k * blockDim.x;
+        if (i < n) {
+          propagate_surface<ML>(sys, S, r[k]);
+          if (ACC) store_ray<false>(a.out, (int64_t)s * a.out.surface_stride + i, S.to_output, r[k]);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int64_t i = base + (int64_t)k * blockDim.x;
+      if (i < n) {
+        if (bin) bin_ray(sys.sensor, a.img, r[k]);
+        if (!ACC) {
+          if (final_identity)
+            store_ray<true>(a.out, i, sys.final_to_output, r[k]);
+          else
+            store_ray<false>(a.out, i, sys.final_to_output, r[k]);
+        }
+      }
+    }
+  }
+}
+
+template <int MODE, bool ML>
+void launch_ml(int rpt, bool acc, int grid, int block, const otx_system& sys,
+               const TraceArgs& a, cudaStream_t st) {
+  if (acc) {
+    if (rpt == 2)
+      k_trace<2, MODE, true, ML><<<grid, block, 0, st>>>(sys, a);
+    else
+      k_trace<1, MODE, true, ML><<<grid, block, 0, st>>>(sys, a);
+  } else {
+    if (rpt == 2)
+      k_trace<2, MODE, false, ML><<<grid, block, 0, st>>>(sys, a);
+    else
+      k_trace<1, MODE, false, ML><<<grid, block, 0, st>>>(sys, a);
+  }
+}
+
+// Launch of one input mode; rays_per_thread is 1 or 2; `ml` selects the
+// variant able to evaluate layered multilayer stacks.
+template <int MODE>
+void launch_mode(int rpt, bool acc, bool ml, int grid, int block, const otx_system& sys,
+                 const TraceArgs& a, cudaStream_t st) {
+  if (ml)
+    launch_ml<MODE, true>(rpt, acc, grid, block, sys, a, st);
+  else
+    launch_ml<MODE, false>(rpt, acc, grid, block, sys, a, st);
+}
+
+}  // namespace otx

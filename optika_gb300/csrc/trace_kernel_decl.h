@@ -1,0 +1,33 @@
+// Declarations of the per-mode launchers (defined in trace_kernel.cuh and
+// explicitly instantiated in trace_rays.cu / trace_grid_inf.cu /
+// trace_grid_fin.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/optika_gb300.h"
+
+namespace otx {
+
+struct TraceArgs {
+  otx_rays in;
+  otx_grid grid;
+  otx_rays out;
+  otx_image img;
+  int64_t count;
+};
+
+template <int MODE>
+void launch_mode(int rpt, bool acc, bool ml, int grid, int block, const otx_system& sys,
+                 const TraceArgs& a, cudaStream_t st);
+
+extern template void launch_mode<OTX_INPUT_RAYS>(int, bool, bool, int, int, const otx_system&,
+                                                 const TraceArgs&, cudaStream_t);
+extern template void launch_mode<OTX_INPUT_GRID_INFINITY>(int, bool, bool, int, int,
+                                                          const otx_system&,
+                                                          const TraceArgs&, cudaStream_t);
+extern template void launch_mode<OTX_INPUT_GRID_FINITE>(int, bool, bool, int, int,
+                                                        const otx_system&,
+                                                        const TraceArgs&, cudaStream_t);
+
+}  // namespace otx

@@ -1,0 +1,79 @@
+"""Imaging sensors, mirroring optika/sensors/_sensors.py.
+
+An :class:`ImagingSensor` is the last surface of a system: flat, vacuum
+(the ideal sensor material, optika/sensors/materials/_materials.py:1567),
+with the pixel array as its aperture (:84-90).  Binning
+(:meth:`ImagingSensor.collect`, :92-171) counts the unvignetted rays and
+sums their intensity per pixel on the GPU; images are laid out as
+``[num_wavelength, num_pixel_x, num_pixel_y]`` with pixel edges
+``linspace(-half_width, +half_width, num + 1)`` (numpy.histogramdd
+semantics: the last edge is inclusive, everything outside is dropped).
+"""
+
+from __future__ import annotations
+
+import dataclasses
+
+import numpy as np
+
+from . import apertures as _apertures
+from . import materials as _materials
+from . import sags as _sags
+from . import transforms
+from .surfaces import AbstractSurface
+
+__all__ = ["ImagingSensor", "IdealSensorMaterial"]
+
+
+class IdealSensorMaterial(_materials.Vacuum):
+    """Unit quantum efficiency; behaves as vacuum in the trace."""
+
+
+@dataclasses.dataclass(eq=False)
+class ImagingSensor(AbstractSurface):
+    name: None | str = None
+    width_pixel: float | tuple[float, float] = 0.0  # mm
+    axis_pixel: tuple[str, str] = ("detector_x", "detector_y")
+    num_pixel: tuple[int, int] = (0, 0)
+    timedelta_exposure: float = 0.0
+    read_noise: float = 0.0
+    material: None | _materials.AbstractMaterial = None
+    aperture_mechanical: None | _apertures.AbstractAperture = None
+    is_field_stop: bool = False
+    is_pupil_stop: bool = False
+    transformation: None | transforms.AbstractTransformation = None
+
+    def __post_init__(self):
+        if self.material is None:
+            self.material = IdealSensorMaterial()
+
+    @property
+    def sag(self) -> _sags.NoSag:
+        return _sags.NoSag()
+
+    @property
+    def rulings(self):
+        return None
+
+    @property
+    def width_pixel_xy(self) -> tuple[float, float]:
+        w = self.width_pixel
+        if np.ndim(w) == 0:
+            return float(w), float(w)
+        return float(w[0]), float(w[1])
+
+    @property
+    def aperture(self) -> _apertures.RectangularAperture:
+        wx, wy = self.width_pixel_xy
+        nx, ny = self.num_pixel
+        return _apertures.RectangularAperture(half_width=(wx * nx / 2, wy * ny / 2))
+
+    def collect(self, rays, wavelength=None, where=True):
+        """Bin rays (in this sensor's local frame) into ``(counts, flux)``.
+
+        ``wavelength`` is ``None`` (one bin, all wavelengths) or
+        ``(start, stop, num)`` uniform wavelength edges in nm.
+        """
+        from ._api import collect
+
+        return collect(self, rays, wavelength=wavelength, where=where)

@@ -1,0 +1,69 @@
+"""Generate ``multilayer_imd.npz`` from the reference's IMD golden data.
+
+The reference pins ``multilayer_efficiency`` against IMD output files
+(optika/materials/_tests/test_multilayers.py:178-287, data in
+optika/materials/_tests/_data/*.txt, normal incidence, rtol 1e-4), computed
+with the optical constants of optika/chemicals/nk/*.nk.  This script reads
+both from a reference checkout (default /root/reference), keeps every
+``STEP``-th wavelength, and stores per case the IMD efficiency and, for each
+chemical of the stack, n and k linearly interpolated at those wavelengths
+(the reference's ``na.interp`` of the table, optika/chemicals/_chemicals.py:
+138-142).  Run it where the reference is available:
+
+    python tests/golden/make_golden.py [/path/to/reference]
+"""
+
+from __future__ import annotations
+
+import pathlib
+import sys
+
+import numpy as np
+
+STEP = 5
+
+CASES = {
+    # name: (IMD file, [(chemical, thickness nm)], substrate chemical, is_mirror)
+    "Si": ("Si.txt", [], "Si", False),
+    "SiO2_50A": ("SiO2.txt", [("SiO2", 5.0)], "Si", False),
+    "SiO2_100A": ("SiO2_100A.txt", [("SiO2", 10.0)], "Si", False),
+    "SiC_Cr": ("SiC_Cr.txt", [("SiC", 25.0), ("Cr", 5.0)], "SiO2", True),
+}
+
+
+def read_columns(path: pathlib.Path) -> np.ndarray:
+    rows = []
+    for line in path.read_text().splitlines():
+        s = line.strip()
+        if not s or s.startswith(";"):
+            continue
+        rows.append([float(v) for v in s.split()])
+    return np.asarray(rows, dtype=np.float64)
+
+
+def main(ref: pathlib.Path) -> None:
+    data_dir = ref / "optika" / "materials" / "_tests" / "_data"
+    nk_dir = ref / "optika" / "chemicals" / "nk"
+    out = {}
+    for name, (fname, layers, substrate, is_mirror) in CASES.items():
+        a = read_columns(data_dir / fname)
+        wl_nm = a[::STEP, 0] / 10.0
+        eff = a[::STEP, 1]
+        out[f"{name}/wavelength"] = wl_nm
+        out[f"{name}/efficiency"] = eff
+        out[f"{name}/is_mirror"] = np.array(is_mirror)
+        out[f"{name}/thickness"] = np.array([t for _, t in layers], dtype=np.float64)
+        chems = [c for c, _ in layers] + [substrate]
+        for i, chem in enumerate(chems):
+            t = read_columns(nk_dir / f"{chem}.nk")
+            w = t[:, 0] / 10.0
+            out[f"{name}/n{i}"] = np.interp(wl_nm, w, t[:, 1])
+            out[f"{name}/k{i}"] = np.interp(wl_nm, w, t[:, 2])
+        out[f"{name}/num_chemicals"] = np.array(len(chems))
+    dst = pathlib.Path(__file__).resolve().parent / "multilayer_imd.npz"
+    np.savez_compressed(dst, **out)
+    print(f"wrote {dst} ({dst.stat().st_size} bytes)")
+
+
+if __name__ == "__main__":
+    main(pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))

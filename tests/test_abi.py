@@ -1,0 +1,136 @@
+"""The C-ABI library: builds, loads, exports every declared symbol, matches
+the ctypes layouts, and rejects bad descriptors on the host (no GPU work)."""
+
+import ctypes
+import pathlib
+import re
+
+import pytest
+
+from optika_gb300 import _lib as L
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"\b(otx_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+def test_every_declared_symbol_is_exported(built_library):
+    names = declared_symbols()
+    assert "otx_trace_grid" in names and "otx_trace_rays" in names
+    for n in names:
+        assert hasattr(built_library, n), f"{n} declared in include/ but not exported"
+
+
+def test_layouts_match(built_library):
+    L.check_layout()
+    for which, cls in L.LAYOUT.items():
+        assert built_library.otx_sizeof(which) == ctypes.sizeof(cls)
+    assert built_library.otx_sizeof(99) == -1
+    # the system descriptor is passed as a kernel parameter (<= 32 KB)
+    assert ctypes.sizeof(L.System) < 32 * 1024
+
+
+def test_status_strings(built_library):
+    for s in range(6):
+        assert built_library.otx_status_string(s)
+
+
+def _system(n=1):
+    s = L.System()
+    s.abi_version = L.ABI_VERSION
+    s.num_surfaces = n
+    s.input_mode = L.INPUT_GRID_INFINITY
+    for k in range(L.MAX_LAYERS):
+        s.layers[k].table = -1
+    for k in range(L.MAX_STACKS):
+        s.stacks[k].substrate = -1
+    return s
+
+
+def _call_rays(lib, sys_, count=0):
+    rin = L.Rays()
+    rin.count = count
+    rout = L.Rays()
+    return lib.otx_trace_rays(ctypes.byref(sys_), ctypes.byref(rin), ctypes.byref(rout), None,
+                              None, None)
+
+
+@pytest.mark.parametrize(
+    "mutate,expected",
+    [
+        (lambda s: setattr(s, "abi_version", 0), L.ERR_INVALID),
+        (lambda s: setattr(s, "num_surfaces", 0), L.ERR_SIZE),
+        (lambda s: setattr(s, "num_surfaces", L.MAX_SURFACES + 1), L.ERR_SIZE),
+        (lambda s: setattr(s.surfaces[0], "sag_type", 99), L.ERR_UNSUPPORTED),
+        (lambda s: setattr(s.surfaces[0], "mat_type", 99), L.ERR_UNSUPPORTED),
+        (lambda s: setattr(s.surfaces[0], "aper_type", 99), L.ERR_UNSUPPORTED),
+        (lambda s: setattr(s.surfaces[0], "rule_type", 99), L.ERR_UNSUPPORTED),
+        (lambda s: (setattr(s.surfaces[0], "mat_type", L.MAT_MULTILAYER_MIRROR),
+                    setattr(s.surfaces[0], "mat_stack", 7)), L.ERR_INVALID),
+        (lambda s: (setattr(s.surfaces[0], "aper_type", L.APER_POLYGON),
+                    setattr(s.surfaces[0], "aper_vertex_count", 2)), L.ERR_INVALID),
+        (lambda s: (setattr(s.surfaces[0], "rule_type", L.RULE_POLY1D),
+                    setattr(s.surfaces[0], "rule_num_terms", 9)), L.ERR_SIZE),
+        (lambda s: setattr(s.layers[0], "table", 3), L.ERR_INVALID),
+        (lambda s: (setattr(s.stacks[0], "pre_count", 5),
+                    setattr(s.stacks[0], "pre_begin", L.MAX_LAYERS - 2)), L.ERR_INVALID),
+    ],
+)
+def test_bad_descriptors_rejected(built_library, mutate, expected):
+    s = _system()
+    mutate(s)
+    assert _call_rays(built_library, s) == expected
+
+
+def test_empty_input_is_ok_without_launch(built_library):
+    assert _call_rays(built_library, _system(), count=0) == L.OK
+
+
+def test_missing_pointers_rejected(built_library):
+    assert _call_rays(built_library, _system(), count=10) == L.ERR_INVALID
+    g = L.Grid()
+    g.count = 5
+    out = L.Rays()
+    s = _system()
+    assert built_library.otx_trace_grid(ctypes.byref(s), ctypes.byref(g), ctypes.byref(out),
+                                        None, None, None) == L.ERR_INVALID
+    s.input_mode = L.INPUT_RAYS
+    g.count = 0
+    assert built_library.otx_trace_grid(ctypes.byref(s), ctypes.byref(g), ctypes.byref(out),
+                                        None, None, None) == L.ERR_INVALID
+
+
+def test_bad_launch_and_image(built_library):
+    s = _system()
+    rin = L.Rays()
+    rin.count = 0
+    out = L.Rays()
+    img = L.Image()
+    img.counts = 1  # non-null: the sensor must then be valid
+    assert built_library.otx_trace_rays(ctypes.byref(s), ctypes.byref(rin), ctypes.byref(out),
+                                        ctypes.byref(img), None, None) == L.ERR_INVALID
+    ln = L.Launch()
+    ln.rays_per_thread = 3
+    assert built_library.otx_trace_rays(ctypes.byref(s), ctypes.byref(rin), ctypes.byref(out),
+                                        None, ctypes.byref(ln), None) in (L.OK, L.ERR_INVALID)
+
+
+def test_collect_and_sag_validation(built_library):
+    sen = L.Sensor()
+    r = L.Rays()
+    img = L.Image()
+    assert built_library.otx_collect(ctypes.byref(sen), ctypes.byref(r), ctypes.byref(img),
+                                     None) == L.ERR_INVALID
+    s = _system()
+    assert built_library.otx_sag_eval(ctypes.byref(s), 5, ctypes.byref(r), ctypes.byref(r),
+                                      None) == L.ERR_INVALID
+    s.surfaces[0].sag_type = 42
+    assert built_library.otx_sag_eval(ctypes.byref(s), 0, ctypes.byref(r), ctypes.byref(r),
+                                      None) == L.ERR_UNSUPPORTED
