@@ -76,14 +76,19 @@ typedef int32_t otx_status;
 
 /* ---- descriptors ----------------------------------------------------- */
 
-/* Rigid affine map x' = m x + (t_hi + t_lo).  Composed on the host in
- * float64 and split into a float-float translation so that the large
- * offsets between surfaces are added without rounding. */
+/* Rigid affine map x' = (m + m_lo) x + (t_hi + t_lo).  Composed on the
+ * host in float64 and split into float-float parts so that the large
+ * offsets between surfaces are added, and directions rotated, without
+ * FP32 rounding. */
+#define OTX_AFFINE_ROT_IDENTITY 1 /* m is exactly the identity           */
 typedef struct otx_affine {
-  float m[9]; /* row-major 3x3 rotation */
+  float m[9];    /* row-major 3x3 rotation, high parts */
+  float m_lo[9]; /* low parts                          */
   float t_hi[3];
   float t_lo[3];
-} otx_affine; /* 60 bytes */
+  int32_t flags;
+  int32_t pad_;
+} otx_affine; /* 104 bytes */
 
 /* Complex refractive index source of one layer or substrate.  A negative
  * `table` means the constant n_re + i n_im; otherwise the index of a
@@ -216,7 +221,7 @@ typedef struct otx_launch {
   int32_t rays_per_thread; /* 1, 2 or 4; 0 = library default          */
   int32_t block_size;      /* threads per CTA; 0 = library default     */
   int32_t accumulate;      /* 1: write every surface's rays            */
-  int32_t pad_;
+  int32_t generic_only;    /* 1: never use a shape-specialised kernel  */
 } otx_launch;
 
 /* ---- entry points ---------------------------------------------------- */

@@ -41,8 +41,18 @@ i64 = ctypes.c_int64
 u64 = ctypes.c_uint64
 
 
+AFFINE_ROT_IDENTITY = 1
+
+
 class Affine(ctypes.Structure):
-    _fields_ = [("m", f32 * 9), ("t_hi", f32 * 3), ("t_lo", f32 * 3)]
+    _fields_ = [
+        ("m", f32 * 9),
+        ("m_lo", f32 * 9),
+        ("t_hi", f32 * 3),
+        ("t_lo", f32 * 3),
+        ("flags", i32),
+        ("pad_", i32),
+    ]
 
 
 class Layer(ctypes.Structure):
@@ -186,7 +196,7 @@ class Launch(ctypes.Structure):
         ("rays_per_thread", i32),
         ("block_size", i32),
         ("accumulate", i32),
-        ("pad_", i32),
+        ("generic_only", i32),
     ]
 
 

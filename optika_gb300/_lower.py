@@ -34,11 +34,14 @@ def set_affine(dst: L.Affine, m: np.ndarray) -> None:
     r = m[:3, :3]
     t = m[:3, 3]
     for i in range(9):
-        dst.m[i] = float(r.flat[i])
+        hi, lo = split_f64(float(r.flat[i]))
+        dst.m[i] = hi
+        dst.m_lo[i] = lo
     for i in range(3):
         hi, lo = split_f64(float(t[i]))
         dst.t_hi[i] = hi
         dst.t_lo[i] = lo
+    dst.flags = L.AFFINE_ROT_IDENTITY if np.array_equal(r, np.eye(3)) else 0
 
 
 class Lowering:

@@ -56,11 +56,11 @@ __global__ void k_sag(const __grid_constant__ otx_system sys, const int mode,
     const float y = reinterpret_cast<const float*>(in.py)[i];
     if (mode == 0) {
       float gx, gy;
-      float z = sag_eval(s, x, y, gx, gy);
+      float z = sag_eval(s.sag_type, s, x, y, gx, gy);
       reinterpret_cast<float*>(out.pz)[i] = z;
     } else if (mode == 1) {
-      float nx, ny, nz;
-      normal(s, x, y, nx, ny, nz);
+      float nx, ny, nz, v[3];
+      normal(s.sag_type, s, x, y, nx, ny, nz, v);
       reinterpret_cast<float*>(out.dx)[i] = nx;
       reinterpret_cast<float*>(out.dy)[i] = ny;
       reinterpret_cast<float*>(out.dz)[i] = nz;
@@ -71,7 +71,8 @@ __global__ void k_sag(const __grid_constant__ otx_system sys, const int mode,
       const float uz = reinterpret_cast<const float*>(in.dz)[i];
       const float lo[3] = {0.f, 0.f, 0.f};
       float px, py, pz;
-      intercept(s, sys.newton_iterations, x, y, z0, lo, ux, uy, uz, px, py, pz);
+      intercept(s.sag_type, s, sys.newton_iterations, x, y, z0, lo, ux, uy, uz, 0.f, 0.f, 0.f,
+                px, py, pz);
       reinterpret_cast<float*>(out.px)[i] = px;
       reinterpret_cast<float*>(out.py)[i] = py;
       reinterpret_cast<float*>(out.pz)[i] = pz;

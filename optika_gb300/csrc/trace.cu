@@ -107,6 +107,8 @@ static otx_status launch_trace(const otx_system* sys_in, int mode, const TraceAr
         ml = true;
     }
   }
+  if (!(launch && launch->generic_only) && launch_fixed(mode, acc, rpt, grid, block, *sys, a, st))
+    return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
   switch (mode) {
     case OTX_INPUT_RAYS:
       launch_mode<OTX_INPUT_RAYS>(rpt, acc, ml, grid, block, *sys, a, st);

@@ -20,7 +20,8 @@ namespace otx {
 
 struct Ray {
   float px, py, pz;      // position in the current frame (mm)
-  float dx, dy, dz;      // direction cosines
+  float dx, dy, dz;      // direction cosines (high parts)
+  float lx, ly, lz;      // direction low parts (float-float direction)
   float wl;              // wavelength (nm)
   float inten;           // intensity
   float att;             // attenuation coefficient (1/mm)
@@ -91,19 +92,73 @@ __device__ __forceinline__ void affine_point_folded(const otx_affine& f,
   z += lo[2];
 }
 
+// One row of a rotation with float-float entries applied to a float-float
+// vector: products split exactly by FMA, sums by TwoSum (Ogita-Rump-Oishi
+// Dot2); returns a float-float pair.
+__device__ __forceinline__ void rot_row_ff(const float* mh, const float* ml, float x, float y,
+                                           float z, float xl, float yl, float zl, float& hi,
+                                           float& lo) {
+  const float p1 = mh[0] * x, e1 = fmaf(mh[0], x, -p1);
+  const float p2 = mh[1] * y, e2 = fmaf(mh[1], y, -p2);
+  const float p3 = mh[2] * z, e3 = fmaf(mh[2], z, -p3);
+  float s, t1, s2, t2;
+  two_sum(p1, p2, s, t1);
+  two_sum(s, p3, s2, t2);
+  float l = (t1 + t2) + (e1 + e2 + e3);
+  l = fmaf(ml[0], x, fmaf(ml[1], y, fmaf(ml[2], z, l)));
+  l = fmaf(mh[0], xl, fmaf(mh[1], yl, fmaf(mh[2], zl, l)));
+  hi = s2 + l;
+  lo = l - (hi - s2);
+}
+
+// Frame change of a ray: position (x, y, z) -> (x, y, z) + lo in the new
+// frame, direction (float-float) rotated.  Pure translations (the common
+// case) add the translation only; rotations are compensated, because an
+// FP32-rounded direction component (~3e-8 for 0.7) would act over the
+// whole incoming segment (hundreds of mm) before the intercept.
+__device__ __forceinline__ void frame_change(const otx_affine& f, Ray& r, float lo[3]) {
+  float px = r.px, py = r.py, pz = r.pz;
+  float rh[3], rl[3];
+  if (f.flags & OTX_AFFINE_ROT_IDENTITY) {
+    rh[0] = px;
+    rh[1] = py;
+    rh[2] = pz;
+    rl[0] = rl[1] = rl[2] = 0.f;
+  } else {
+    for (int i = 0; i < 3; ++i)
+      rot_row_ff(f.m + 3 * i, f.m_lo + 3 * i, px, py, pz, 0.f, 0.f, 0.f, rh[i], rl[i]);
+    float dh[3], dl[3];
+    for (int i = 0; i < 3; ++i)
+      rot_row_ff(f.m + 3 * i, f.m_lo + 3 * i, r.dx, r.dy, r.dz, r.lx, r.ly, r.lz, dh[i], dl[i]);
+    r.dx = dh[0];
+    r.dy = dh[1];
+    r.dz = dh[2];
+    r.lx = dl[0];
+    r.ly = dl[1];
+    r.lz = dl[2];
+  }
+  float e;
+  two_sum(rh[0], f.t_hi[0], r.px, e);
+  lo[0] = e + (rl[0] + f.t_lo[0]);
+  two_sum(rh[1], f.t_hi[1], r.py, e);
+  lo[1] = e + (rl[1] + f.t_lo[1]);
+  two_sum(rh[2], f.t_hi[2], r.pz, e);
+  lo[2] = e + (rl[2] + f.t_lo[2]);
+}
+
 // ---------------------------------------------------------------- sags
 
 // Sag z(x, y) and its gradient for the curved sag types.
 // Conic: optika/sags/_conic.py:31-48 (sag), :50-75 (gradient c x / g).
 // Toroid: optika/sags/_toroidal.py:38-57 (sag), :59-88 (gradient).
-__device__ __forceinline__ float sag_eval(const otx_surface& s, float x,
+__device__ __forceinline__ float sag_eval(int sag_type, const otx_surface& s, float x,
                                           float y, float& gx, float& gy) {
-  switch (s.sag_type) {
+  switch (sag_type) {
     case OTX_SAG_SPHERE:
     case OTX_SAG_CONIC:
     case OTX_SAG_PARABOLA: {
       const float c = s.sag_curvature;
-      const float kp1 = (s.sag_type == OTX_SAG_SPHERE) ? 1.f : 1.f + s.sag_conic;
+      const float kp1 = (sag_type == OTX_SAG_SPHERE) ? 1.f : 1.f + s.sag_conic;
       const float r2 = fmaf(x, x, y * y);
       const float g = sqrtf(1.f - kp1 * c * c * r2);
       const float cg = c / g;
@@ -122,6 +177,9 @@ __device__ __forceinline__ float sag_eval(const otx_surface& s, float x,
       const float inv_f = 1.f / f;
       gx = x * inv_f;
       gy = rz * (c * y / g) * inv_f;
+      // r - f = (r^2 - f^2) / (r + f) = (z_y (2 r - z_y) + x^2) / (r + f),
+      // free of the cancellation of r - f when f ~ r > 0
+      if (r >= 0.f) return fmaf(zy, 2.f * r - zy, x * x) / (r + f);
       return r - f;
     }
     default:
@@ -132,11 +190,11 @@ __device__ __forceinline__ float sag_eval(const otx_surface& s, float x,
 }
 
 // One Newton step on f(t) = z(t) - sag(x(t), y(t)) from the current point.
-__device__ __forceinline__ float newton_step(const otx_surface& s, float& x,
+__device__ __forceinline__ float newton_step(int sag_type, const otx_surface& s, float& x,
                                              float& y, float& z, float ux,
                                              float uy, float uz) {
   float gx, gy;
-  const float zs = sag_eval(s, x, y, gx, gy);
+  const float zs = sag_eval(sag_type, s, x, y, gx, gy);
   const float f = z - zs;
   const float fp = uz - (gx * ux + gy * uy);
   const float dt = f / fp;
@@ -159,18 +217,23 @@ __device__ __forceinline__ float newton_step(const otx_surface& s, float& x,
 //   toroid    optika/sags/_abc.py:76-107 (iterative root near the vertex
 //             plane; here Newton from the plane intercept)
 // The closed forms use the cancellation-free product-of-roots identity.
-__device__ __forceinline__ float intercept(const otx_surface& s,
+//
+// The direction's low parts (lx, ly, lz) enter only the intercept point
+// (o_hi + t u_hi) + (o_lo + t u_lo), where they act over the full segment.
+__device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
                                            int newton_max, float ox, float oy,
                                            float oz, const float lo[3],
                                            float ux, float uy, float uz,
+                                           float lx, float ly, float lz,
                                            float& x, float& y, float& z) {
   const float oxf = ox + lo[0], oyf = oy + lo[1], ozf = oz + lo[2];
-  if (s.sag_type == OTX_SAG_FLAT) {
+  if (sag_type == OTX_SAG_FLAT) {
     const float inv = 1.f / uz;
-    const float t = -ozf * inv;
-    x = fmaf(t, ux, ox) + lo[0];
-    y = fmaf(t, uy, oy) + lo[1];
-    z = fmaf(t, uz, oz) + lo[2];
+    const float t0 = -ozf * inv;
+    const float t = t0 - (t0 * lz) * inv;  // first order in u_lo
+    x = fmaf(t, ux, ox) + fmaf(t, lx, lo[0]);
+    y = fmaf(t, uy, oy) + fmaf(t, ly, lo[1]);
+    z = fmaf(t, uz, oz) + fmaf(t, lz, lo[2]);
     const float dt = z * inv;  // Newton step on z = 0
     x = fmaf(-dt, ux, x);
     y = fmaf(-dt, uy, y);
@@ -178,7 +241,7 @@ __device__ __forceinline__ float intercept(const otx_surface& s,
     return t - dt;
   }
   float t;
-  switch (s.sag_type) {
+  switch (sag_type) {
     case OTX_SAG_SPHERE: {
       const float R = s.sag_radius;
       // p = o - (0, 0, R); b = u.p; cc = |p|^2 - R^2 = |o|^2 - 2 o_z R
@@ -250,15 +313,15 @@ __device__ __forceinline__ float intercept(const otx_surface& s,
       t = -ozf / uz;
       break;
   }
-  // point on the ray, small coordinates: (o_hi + t u) + o_lo
-  x = fmaf(t, ux, ox) + lo[0];
-  y = fmaf(t, uy, oy) + lo[1];
-  z = fmaf(t, uz, oz) + lo[2];
-  if (s.sag_type == OTX_SAG_TOROID) {
+  // point on the ray, small coordinates: (o_hi + t u) + (o_lo + t u_lo)
+  x = fmaf(t, ux, ox) + fmaf(t, lx, lo[0]);
+  y = fmaf(t, uy, oy) + fmaf(t, ly, lo[1]);
+  z = fmaf(t, uz, oz) + fmaf(t, lz, lo[2]);
+  if (sag_type == OTX_SAG_TOROID) {
     const int iters = newton_max > 0 ? newton_max : 12;
     bool conv = false;
     for (int i = 0; i < iters; ++i) {
-      const float dt = newton_step(s, x, y, z, ux, uy, uz);
+      const float dt = newton_step(sag_type, s, x, y, z, ux, uy, uz);
       t -= dt;
       if (fabsf(dt) <= 1e-7f * (1.f + fabsf(t))) {
         conv = true;
@@ -269,7 +332,7 @@ __device__ __forceinline__ float intercept(const otx_surface& s,
       x = y = z = NAN;
     }
   } else if (isfinite(t)) {
-    t -= newton_step(s, x, y, z, ux, uy, uz);
+    t -= newton_step(sag_type, s, x, y, z, ux, uy, uz);
   }
   return t;
 }
@@ -280,50 +343,113 @@ __device__ __forceinline__ float intercept(const otx_surface& s,
 //   conic    optika/sags/_conic.py:50-75
 //   parabola optika/sags/_parabolic.py:40-63 (equal to the k = -1 conic)
 //   toroid   optika/sags/_toroidal.py:59-88
-__device__ __forceinline__ void normal(const otx_surface& s, float x, float y,
-                                       float& nx, float& ny, float& nz) {
-  switch (s.sag_type) {
+//
+// v receives a vector parallel to the normal that is exact up to the
+// rounding of its components (the unnormalised gradient (g_x, g_y, -1), or
+// for the sphere the normal itself); curved mirrors reflect off v.
+__device__ __forceinline__ void normal(int sag_type, const otx_surface& s, float x, float y,
+                                       float& nx, float& ny, float& nz, float v[3]) {
+  switch (sag_type) {
     case OTX_SAG_SPHERE: {
       const float c = s.sag_curvature;
       nx = c * x;
       ny = c * y;
       nz = -sqrtf(1.f - nx * nx - ny * ny);
+      v[0] = nx;
+      v[1] = ny;
+      v[2] = nz;
       return;
     }
     case OTX_SAG_CONIC:
     case OTX_SAG_PARABOLA:
     case OTX_SAG_TOROID: {
       float gx, gy;
-      sag_eval(s, x, y, gx, gy);
-      const float inv = rsqrtf(fmaf(gx, gx, fmaf(gy, gy, 1.f)));
+      sag_eval(sag_type, s, x, y, gx, gy);
+      // 1 / |(gx, gy, -1)|: the hardware estimate refined by one Newton step
+      const float q = fmaf(gx, gx, fmaf(gy, gy, 1.f));
+      float inv = rsqrtf(q);
+      inv = fmaf(0.5f * inv, fmaf(-q * inv, inv, 1.f), inv);
       nx = gx * inv;
       ny = gy * inv;
       nz = -inv;
+      v[0] = gx;
+      v[1] = gy;
+      v[2] = -1.f;
       return;
     }
     default:
       nx = 0.f;
       ny = 0.f;
       nz = -1.f;
+      v[0] = 0.f;
+      v[1] = 0.f;
+      v[2] = -1.f;
       return;
   }
 }
 
 // ---------------------------------------------------------------- Snell
 
+// Compensated dot product a.u (Ogita-Rump-Oishi Dot2: products split
+// exactly by FMA, sums by TwoSum); accurate to ~1 ulp of the result.
+__device__ __forceinline__ float dot3_compensated(float ax, float ay, float az, float ux,
+                                                  float uy, float uz) {
+  const float p1 = az * uz, e1 = fmaf(az, uz, -p1);
+  const float p2 = ay * uy, e2 = fmaf(ay, uy, -p2);
+  const float p3 = ax * ux, e3 = fmaf(ax, ux, -p3);
+  float s, t1, s2, t2;
+  two_sum(p1, p2, s, t1);
+  two_sum(s, p3, s2, t2);
+  return s2 + ((t1 + t2) + (e1 + e2 + e3));
+}
+
+// Scale a (near-)unit float-float vector to unit length when its length
+// differs from 1 by more than FP32 rounding (reciprocal square root refined
+// by one Newton step); a vector already unit to rounding is left as is.
+__device__ __forceinline__ void normalize3(float& x, float& y, float& z, float& lx, float& ly,
+                                           float& lz) {
+  float e = fmaf(x, x, -1.f);
+  e = fmaf(y, y, e);
+  e = fmaf(z, z, e);
+  e += 2.f * fmaf(x, lx, fmaf(y, ly, z * lz));
+  if (fabsf(e) < 3e-7f) return;
+  const float q = 1.f + e;
+  float inv = rsqrtf(q);
+  inv = fmaf(0.5f * inv, fmaf(-q * inv, inv, 1.f), inv);
+  x *= inv;
+  y *= inv;
+  z *= inv;
+  lx *= inv;
+  ly *= inv;
+  lz *= inv;
+}
+
 // Vector Snell's law, optika/materials/_snells_law.py:341-366:
 //   d = -a.u + sgn (2 m - 1) sqrt(1/r^2 + (a.u)^2 - |a|^2),  b = r (a + d u)
 // with sgn = -copysign(1, a.u).  The radicand's (1/r^2 - |a|^2) is formed
-// as ((n2/n1)^2 - 1) - (|a|^2 - 1) with fused multiply-adds so that unit
-// directions reflect without the 1 - |a|^2 rounding of a plain FP32 sum;
-// equal indices (mirrors, vacuum to vacuum) skip the divisions (r = 1).
-__device__ __forceinline__ void snell(float& ax, float& ay, float& az, float n1,
-                                      float n2, bool mirror, float ux,
+// as ((n2/n1)^2 - 1) - (|a|^2 - 1) with fused multiply-adds, and a.u is a
+// compensated dot product: a rounding error in a.u would otherwise leave
+// the reflected direction off unit length along the normal, and the next
+// surface would turn that into a transverse error.  A direction whose
+// |a|^2 differs from 1 by less than 1e-6 is unit up to FP32 rounding (the
+// reference's float64 directions are unit to 1e-16): that residue is
+// dropped instead of being folded into the normal component, and a unit
+// ray crossing equal indices without reflection leaves unchanged (the
+// formula's d is then 0).  Effective grating directions (|a|^2 - 1 ~ 1e-2)
+// keep their residue.  Equal indices skip the divisions (r = 1).
+__device__ __forceinline__ void snell(float& ax, float& ay, float& az, float& lx, float& ly,
+                                      float& lz, float n1, float n2, bool mirror, float ux,
                                       float uy, float uz) {
   float e = fmaf(ax, ax, -1.f);
   e = fmaf(ay, ay, e);
   e = fmaf(az, az, e);
-  const float au = fmaf(ax, ux, fmaf(ay, uy, az * uz));
+  const bool unit = fabsf(e) < 1e-6f;
+  if (unit) {
+    if (!mirror && n1 == n2) return;
+    e = 0.f;
+  }
+  const float au = dot3_compensated(ax, ay, az, ux, uy, uz);
+  const float lu = fmaf(lx, ux, fmaf(ly, uy, lz * uz));  // a_lo . u
   const float sgn = -copysignf(1.f, au);
   float r = 1.f, q2m1 = 0.f;
   if (n1 != n2) {
@@ -331,11 +457,88 @@ __device__ __forceinline__ void snell(float& ax, float& ay, float& az, float n1,
     const float q = n2 / n1;
     q2m1 = (q - 1.f) * (q + 1.f);
   }
-  const float rad = fmaf(au, au, q2m1 - e);
-  const float d = -au + sgn * (mirror ? 1.f : -1.f) * sqrtf(rad);
-  ax = r * fmaf(d, ux, ax);
-  ay = r * fmaf(d, uy, ay);
-  az = r * fmaf(d, uz, az);
+  float d, dd;  // d and its first-order change from the low parts
+  if (mirror && unit && n1 == n2) {
+    d = -2.f * au;  // sqrt((a.u)^2) = |a.u| and sgn |a.u| = -a.u
+    dd = -2.f * lu;
+  } else {
+    const float rad = fmaf(au, au, q2m1 - e);
+    const float sq = sqrtf(rad);
+    const float sig = sgn * (mirror ? 1.f : -1.f);
+    d = -au + sig * sq;
+    // d(rad) = 2 (a.u) d(a.u) - 2 a.d(a); d(sq) = d(rad) / (2 sq)
+    const float al = fmaf(ax, lx, fmaf(ay, ly, az * lz));
+    dd = -lu + sig * (au * lu - al) / sq;
+  }
+  const float bx = fmaf(d, ux, ax), by = fmaf(d, uy, ay), bz = fmaf(d, uz, az);
+  lx = r * fmaf(dd, ux, lx);
+  ly = r * fmaf(dd, uy, ly);
+  lz = r * fmaf(dd, uz, lz);
+  ax = r * bx;
+  ay = r * by;
+  az = r * bz;
+  // The formula's b is unit in exact arithmetic for any a (|b|^2 =
+  // r^2 (|a|^2 + 2 d a.u + d^2) = 1); renormalising removes a residue
+  // along the normal beyond FP32 rounding.
+  normalize3(ax, ay, az, lx, ly, lz);
+}
+
+// Reflection off a curved mirror, b = a - 2 (a.v) v / (v.v), with v parallel
+// to the normal but not normalised: the scale k = 2 (a.v) / (v.v) is formed
+// in float-float (compensated dot products and a corrected quotient), so the
+// transverse components of b carry only the rounding of v's components.
+// Equal to the reference's mirror case of Snell's law for unit a.
+__device__ __forceinline__ void reflect_curved(float& ax, float& ay, float& az, float& lx,
+                                               float& ly, float& lz, const float v[3]) {
+  // numerator a.v and denominator v.v as float-float pairs
+  float n_hi, n_lo, d_hi, d_lo;
+  {
+    const float p1 = az * v[2], e1 = fmaf(az, v[2], -p1);
+    const float p2 = ay * v[1], e2 = fmaf(ay, v[1], -p2);
+    const float p3 = ax * v[0], e3 = fmaf(ax, v[0], -p3);
+    float t1, s2, t2, s;
+    two_sum(p1, p2, s, t1);
+    two_sum(s, p3, s2, t2);
+    float lo = (t1 + t2) + (e1 + e2 + e3);
+    lo = fmaf(lx, v[0], fmaf(ly, v[1], fmaf(lz, v[2], lo)));  // + a_lo . v
+    n_hi = s2 + lo;
+    n_lo = lo - (n_hi - s2);
+  }
+  {
+    const float p1 = v[2] * v[2], e1 = fmaf(v[2], v[2], -p1);
+    const float p2 = v[1] * v[1], e2 = fmaf(v[1], v[1], -p2);
+    const float p3 = v[0] * v[0], e3 = fmaf(v[0], v[0], -p3);
+    float t1, s2, t2, s;
+    two_sum(p1, p2, s, t1);
+    two_sum(s, p3, s2, t2);
+    const float lo = (t1 + t2) + (e1 + e2 + e3);
+    d_hi = s2 + lo;
+    d_lo = lo - (d_hi - s2);
+  }
+  // q = n / d in float-float: q_hi = n_hi / d_hi, then one correction
+  const float q_hi = n_hi / d_hi;
+  const float rem = (fmaf(-q_hi, d_hi, n_hi) + n_lo) - q_hi * d_lo;
+  const float q_lo = rem / d_hi;
+  const float k_hi = 2.f * q_hi, k_lo = 2.f * q_lo;
+  // b = a - k v, each component as a float-float pair
+  float b[3], bl[3];
+  const float a[3] = {ax, ay, az}, al[3] = {lx, ly, lz};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float p = k_hi * v[i];
+    const float pe = fmaf(k_hi, v[i], -p);
+    float s, e;
+    two_sum(a[i], -p, s, e);
+    b[i] = s;
+    bl[i] = e + (al[i] - pe - k_lo * v[i]);
+  }
+  ax = b[0];
+  ay = b[1];
+  az = b[2];
+  lx = bl[0];
+  ly = bl[1];
+  lz = bl[2];
+  normalize3(ax, ay, az, lx, ly, lz);
 }
 
 // ---------------------------------------------------------------- rulings
@@ -344,11 +547,11 @@ __device__ __forceinline__ void snell(float& ax, float& ay, float& az, float n1,
 //   constant     optika/rulings/_spacing.py:69-74
 //   polynomial   optika/rulings/_spacing.py:109-128
 //   holographic  optika/rulings/_spacing.py:295-328
-__device__ __forceinline__ void ruling_kappa(const otx_surface& s, float x,
+__device__ __forceinline__ void ruling_kappa(int rule_type, const otx_surface& s, float x,
                                              float y, float z, float nx,
                                              float ny, float nz, float& kx,
                                              float& ky, float& kz) {
-  switch (s.rule_type) {
+  switch (rule_type) {
     case OTX_RULE_CONSTANT: {
       const float d = s.rule_coef[0];
       kx = d * s.rule_normal[0];
@@ -395,11 +598,11 @@ __device__ __forceinline__ void ruling_kappa(const otx_surface& s, float x,
 
 // Effective incident direction, optika/rulings/_rulings.py:124-126:
 //   a + sign(a.n) m lambda g / (n d),  g = kappa / d.
-__device__ __forceinline__ void incident_effective(const otx_surface& s,
+__device__ __forceinline__ void incident_effective(int rule_type, const otx_surface& s,
                                                    Ray& r, float nx, float ny,
                                                    float nz) {
   float kx, ky, kz;
-  ruling_kappa(s, r.px, r.py, r.pz, nx, ny, nz, kx, ky, kz);
+  ruling_kappa(rule_type, s, r.px, r.py, r.pz, nx, ny, nz, kx, ky, kz);
   const float d2 = kx * kx + ky * ky + kz * kz;
   const float an = r.dx * nx + r.dy * ny + r.dz * nz;
   const float w_mm = r.wl * 1e-6f;
@@ -415,14 +618,14 @@ __device__ __forceinline__ void incident_effective(const otx_surface& s,
 // elliptical :640-663, polygonal :739-778, rectangular :941-968.
 // Comparisons are inclusive (<=) as in the reference; NaN coordinates test
 // false before inversion.
-__device__ __forceinline__ bool aperture_inside(const otx_system& sys,
+__device__ __forceinline__ bool aperture_inside(int aper_type, const otx_system& sys,
                                                 const otx_surface& s, float x,
                                                 float y, float z) {
   const int flags = s.aper_flags;
   if (!(flags & OTX_APER_FLAG_ACTIVE)) return true;
   if (flags & OTX_APER_FLAG_TRANSFORM) affine_point_folded(s.aper_to_local, x, y, z);
   bool m;
-  switch (s.aper_type) {
+  switch (aper_type) {
     case OTX_APER_CIRCULAR:
       m = sqrtf(fmaf(x, x, y * y)) <= s.aper_p[0];
       break;
@@ -777,24 +980,40 @@ static __device__ __noinline__ float multilayer_efficiency_call(const otx_system
 
 // ---------------------------------------------------------------- surface
 
+// Compile-time description of one surface: each tag is an OTX_* type, or
+// -1 to read the type from the descriptor at run time.  MAT may also be
+// OTX_MAT_FRESNEL_MIRROR: a multilayer mirror whose stack is a bare
+// substrate.
+#define OTX_MAT_FRESNEL_MIRROR 100
+template <int SAG, int MAT, int APER, int RULE>
+struct Kind {
+  static constexpr int sag = SAG, mat = MAT, aper = APER, rule = RULE;
+};
+using AnyKind = Kind<-1, -1, -1, -1>;
+
 // One surface of optika/surfaces.py:123-198 for a ray already expressed in
 // the previous frame.  Returns with the ray in this surface's frame.  ML
-// selects the kernel variant that can evaluate layered multilayer stacks
-// (chosen by the host when the system has one).
-template <bool ML>
+// selects the variant that can evaluate layered multilayer stacks (chosen
+// by the host when the system has one).
+template <class K, bool ML>
 __device__ __forceinline__ void propagate_surface(const otx_system& sys,
                                                   const otx_surface& s,
                                                   Ray& r) {
+  const int sag_type = K::sag >= 0 ? K::sag : s.sag_type;
+  const int mat_type = K::mat >= 0 ? K::mat : s.mat_type;
+  const int aper_type = K::aper >= 0 ? K::aper : s.aper_type;
+  const int rule_type = K::rule >= 0 ? K::rule : s.rule_type;
+
   // transformation.inverse (surfaces.py:141-142), float-float translation
+  // and compensated rotation
   float lo[3];
-  float ox = r.px, oy = r.py, oz = r.pz;
-  affine_point(s.to_local, ox, oy, oz, lo);
-  rotate(s.to_local, r.dx, r.dy, r.dz);
+  frame_change(s.to_local, r, lo);
+  const float ox = r.px, oy = r.py, oz = r.pz;
 
   // sag.propagate_rays (sags/_abc.py:109-122)
   float x, y, z;
-  const float t = intercept(s, sys.newton_iterations, ox, oy, oz, lo, r.dx,
-                            r.dy, r.dz, x, y, z);
+  const float t = intercept(sag_type, s, sys.newton_iterations, ox, oy, oz, lo, r.dx,
+                            r.dy, r.dz, r.lx, r.ly, r.lz, x, y, z);
   r.px = x;
   r.py = y;
   r.pz = z;
@@ -804,10 +1023,10 @@ __device__ __forceinline__ void propagate_surface(const otx_system& sys,
   }
   opl_add(r, r.n, t);
 
-  float nx, ny, nz;
-  normal(s, x, y, nx, ny, nz);
+  float nx, ny, nz, v[3];
+  normal(sag_type, s, x, y, nx, ny, nz, v);
 
-  if (s.rule_type != OTX_RULE_NONE) incident_effective(s, r, nx, ny, nz);
+  if (rule_type != OTX_RULE_NONE) incident_effective(rule_type, s, r, nx, ny, nz);
 
   // material (surfaces.py:160-181)
   const float n1 = r.n;
@@ -815,7 +1034,7 @@ __device__ __forceinline__ void propagate_surface(const otx_system& sys,
   float att2 = r.att;
   float eff = 1.f;
   bool mirror = false;
-  switch (s.mat_type) {
+  switch (mat_type) {
     case OTX_MAT_VACUUM:
       n2 = 1.f;
       att2 = 0.f;
@@ -832,35 +1051,40 @@ __device__ __forceinline__ void propagate_surface(const otx_system& sys,
       att2 = 0.f;
       break;
     }
+    case OTX_MAT_FRESNEL_MIRROR:
     case OTX_MAT_MULTILAYER_MIRROR:
     case OTX_MAT_MULTILAYER_FILM: {
-      mirror = (s.mat_type == OTX_MAT_MULTILAYER_MIRROR);
+      mirror = (mat_type != OTX_MAT_MULTILAYER_FILM);
       // n = n_ray + i att lambda / (4 pi), cos = -a.n (_multilayers.py:924-932)
       const float k = r.att * (r.wl * 1e-6f) * 0.07957747154594767f;
       const float cos0 = -(r.dx * nx + r.dy * ny + r.dz * nz);
-      const otx_stack& K = sys.stacks[s.mat_stack];
-      if (ML && stack_has_layers(K))
+      const otx_stack& K2 = sys.stacks[s.mat_stack];
+      if (mat_type != OTX_MAT_FRESNEL_MIRROR && ML && stack_has_layers(K2))
         eff = multilayer_efficiency_call(sys, s.mat_stack, mirror, r.wl, cos0, n1, k);
       else
-        eff = fresnel_efficiency(sys, K, mirror, r.wl, cos0, cf{n1, k});
+        eff = fresnel_efficiency(sys, K2, mirror, r.wl, cos0, cf{n1, k});
       break;
     }
     default:
       break;
   }
-  if (s.rule_type != OTX_RULE_NONE) eff *= s.rule_efficiency;
+  if (rule_type != OTX_RULE_NONE) eff *= s.rule_efficiency;
   // wavelength_2 = wavelength_1 / (n1 / n2)   (surfaces.py:162-165)
   if (n2 != n1) r.wl = r.wl / (n1 / n2);
-  snell(r.dx, r.dy, r.dz, n1, n2, mirror, nx, ny, nz);
+  if (mirror && sag_type != OTX_SAG_FLAT && rule_type == OTX_RULE_NONE &&
+      fabsf(fmaf(r.dx, r.dx, fmaf(r.dy, r.dy, fmaf(r.dz, r.dz, -1.f)))) < 1e-6f)
+    reflect_curved(r.dx, r.dy, r.dz, r.lx, r.ly, r.lz, v);
+  else
+    snell(r.dx, r.dy, r.dz, r.lx, r.ly, r.lz, n1, n2, mirror, nx, ny, nz);
   r.inten *= eff;
   r.att = att2;
   r.n = n2;
 
   // aperture.clip_rays (apertures/_apertures.py:82-102)
-  if (s.aper_type != OTX_APER_NONE) {
+  if (aper_type != OTX_APER_NONE) {
     const bool on_dir = (s.aper_flags & OTX_APER_FLAG_DIRECTION) != 0;
-    const bool m = on_dir ? aperture_inside(sys, s, r.dx, r.dy, r.dz)
-                          : aperture_inside(sys, s, r.px, r.py, r.pz);
+    const bool m = on_dir ? aperture_inside(aper_type, sys, s, r.dx, r.dy, r.dz)
+                          : aperture_inside(aper_type, sys, s, r.px, r.py, r.pz);
     r.ok = r.ok && m;
   }
 }

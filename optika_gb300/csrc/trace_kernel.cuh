@@ -35,6 +35,7 @@ __device__ __forceinline__ void load_ray(const TraceArgs& a, int64_t i, Ray& r) 
     r.dx = reinterpret_cast<const float*>(in.dx)[i];
     r.dy = reinterpret_cast<const float*>(in.dy)[i];
     r.dz = reinterpret_cast<const float*>(in.dz)[i];
+    r.lx = r.ly = r.lz = 0.f;
     r.wl = in.wavelength ? reinterpret_cast<const float*>(in.wavelength)[i] : 0.f;
     r.inten = in.intensity ? reinterpret_cast<const float*>(in.intensity)[i] : 1.f;
     r.att = in.attenuation ? reinterpret_cast<const float*>(in.attenuation)[i] : 0.f;
@@ -60,6 +61,7 @@ __device__ __forceinline__ void load_ray(const TraceArgs& a, int64_t i, Ray& r) 
       direction_from_angles(qx, qy, r.dx, r.dy, r.dz);
     }
     r.pz = 0.f;
+    r.lx = r.ly = r.lz = 0.f;
     r.wl = wl;
     r.inten = g.intensity ? reinterpret_cast<const float*>(g.intensity)[i * g.stride_intensity] : 1.f;
     r.att = 0.f;
@@ -74,7 +76,7 @@ template <bool IDENTITY>
 __device__ __forceinline__ void store_ray(const otx_rays& o, int64_t i,
                                           const otx_affine& f, const Ray& r) {
   float x = r.px, y = r.py, z = r.pz;
-  float dx = r.dx, dy = r.dy, dz = r.dz;
+  float dx = r.dx + r.lx, dy = r.dy + r.ly, dz = r.dz + r.lz;
   if (!IDENTITY) {
     affine_point_folded(f, x, y, z);
     rotate(f, dx, dy, dz);
@@ -151,7 +153,7 @@ __global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
       for (int k = 0; k < RPT; ++k) {
         const int64_t i = base + (int64_t)k * blockDim.x;
         if (i < n) {
-          propagate_surface<ML>(sys, S, r[k]);
+          propagate_surface<AnyKind, ML>(sys, S, r[k]);
           if (ACC) store_ray<false>(a.out, (int64_t)s * a.out.surface_stride + i, S.to_output, r[k]);
         }
       }
@@ -170,6 +172,70 @@ __global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
       }
     }
   }
+}
+
+// ---------------------------------------------------------------- fixed shapes
+
+// The whole surface sequence as compile-time kinds: sys.surfaces[I] is read
+// at compile-time offsets (constant-bank operands, no indexed loads) and
+// every type switch folds away.
+template <int I, class K, class... Rest>
+__device__ __forceinline__ void propagate_fixed(const otx_system& sys, Ray& r) {
+  propagate_surface<K, false>(sys, sys.surfaces[I], r);
+  if constexpr (sizeof...(Rest) > 0) propagate_fixed<I + 1, Rest...>(sys, r);
+}
+
+template <int MODE, class... Ks>
+__global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
+    k_trace_fixed(const __grid_constant__ otx_system sys,
+                  const __grid_constant__ TraceArgs a) {
+  const int64_t n = a.count;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  const bool bin = (a.img.counts != 0) || (a.img.flux != 0);
+  const bool final_identity = (sys.flags & OTX_SYS_FLAG_FINAL_IDENTITY) != 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
+    Ray r;
+    load_ray<MODE>(a, i, r);
+    propagate_fixed<0, Ks...>(sys, r);
+    if (bin) bin_ray(sys.sensor, a.img, r);
+    if (final_identity)
+      store_ray<true>(a.out, i, sys.final_to_output, r);
+    else
+      store_ray<false>(a.out, i, sys.final_to_output, r);
+  }
+}
+
+// Kind of surface i as the fixed kernels see it (a multilayer mirror on a
+// bare substrate is the Fresnel mirror kind).
+inline int effective_mat(const otx_system& sys, const otx_surface& s) {
+  if (s.mat_type == OTX_MAT_MULTILAYER_MIRROR) {
+    const otx_stack& K = sys.stacks[s.mat_stack];
+    if (!(K.pre_count > 0 || (K.per_count > 0 && K.num_periods > 0) || K.post_count > 0))
+      return OTX_MAT_FRESNEL_MIRROR;
+  }
+  return s.mat_type;
+}
+
+template <class... Ks>
+bool shape_matches(const otx_system& sys) {
+  constexpr int n = sizeof...(Ks);
+  if (sys.num_surfaces != n) return false;
+  const int sig[n][4] = {{Ks::sag, Ks::mat, Ks::aper, Ks::rule}...};
+  for (int i = 0; i < n; ++i) {
+    const otx_surface& s = sys.surfaces[i];
+    if (s.sag_type != sig[i][0] || effective_mat(sys, s) != sig[i][1] ||
+        s.aper_type != sig[i][2] || s.rule_type != sig[i][3])
+      return false;
+  }
+  return true;
+}
+
+template <int MODE, class... Ks>
+bool try_fixed(int grid, int block, const otx_system& sys, const TraceArgs& a,
+               cudaStream_t st) {
+  if (!shape_matches<Ks...>(sys)) return false;
+  k_trace_fixed<MODE, Ks...><<<grid, block, 0, st>>>(sys, a);
+  return true;
 }
 
 template <int MODE, bool ML>

@@ -30,4 +30,9 @@ extern template void launch_mode<OTX_INPUT_GRID_FINITE>(int, bool, bool, int, in
                                                         const otx_system&,
                                                         const TraceArgs&, cudaStream_t);
 
+// Launch a kernel specialised for the system's shape if one exists
+// (trace_fixed.cu); false when the generic kernel must run.
+bool launch_fixed(int mode, bool acc, int rpt, int grid, int block, const otx_system& sys,
+                  const TraceArgs& a, cudaStream_t st);
+
 }  // namespace otx

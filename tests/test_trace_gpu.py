@@ -23,7 +23,17 @@ pytestmark = pytest.mark.gpu
 V2 = ok.vectors.Cartesian2dVectorArray
 V3 = ok.vectors.Cartesian3dVectorArray
 PIX = 0.0135
-EDGE_PX = 5e-3
+EDGE_PX = 1e-3
+
+
+def f32(g: dict) -> dict:
+    """Inputs rounded to float32, the values the kernel sees; the oracle is
+    given the same values so that only arithmetic differs."""
+    return {k: np.asarray(v, dtype=np.float32).astype(np.float64) for k, v in g.items()}
+
+
+def c32(z: complex) -> complex:
+    return complex(np.float32(z.real), np.float32(z.imag))
 
 
 def run_rayfunction(system, g, **kw):
@@ -55,7 +65,7 @@ def assert_rays_close(out, ref, pos_tol=1.5e-4, dir_tol=2e-6, opl_tol=1e-3, rms_
 
 def test_newtonian_small_workload(cuda):
     s = configs.newtonian()
-    g = configs.newtonian_grid()
+    g = f32(configs.newtonian_grid())
     res = run_rayfunction(s, g, image=True)
     out = res.outputs.numpy()
     ref = oracle_rayfunction(s, g)
@@ -85,7 +95,7 @@ def test_newtonian_small_workload(cuda):
 
 def test_accumulate_matches_per_surface(cuda):
     s = configs.newtonian()
-    g = configs.newtonian_grid(num_pupil=400)
+    g = f32(configs.newtonian_grid(num_pupil=400))
     res = s.raytrace(wavelength=g["wavelength"], field=V2(g["field_x"], g["field_y"]),
                      pupil=V2(g["pupil_x"], g["pupil_y"]), normalized_field=False,
                      normalized_pupil=False, accumulate=True)
@@ -102,7 +112,7 @@ def test_accumulate_matches_per_surface(cuda):
 
 def test_precision_workload_error_budget(cuda):
     s = configs.newtonian(coated=True)
-    g = configs.precision_grid(200_000)
+    g = f32(configs.precision_grid(200_000))
     out = run_rayfunction(s, g).outputs.numpy()
     ref = oracle_rayfunction(s, g)
     assert_rays_close(out, ref)
@@ -112,7 +122,7 @@ def test_precision_workload_error_budget(cuda):
 
 def test_rays_input_equals_grid_input(cuda):
     s = configs.newtonian()
-    g = configs.newtonian_grid(num_pupil=100)
+    g = f32(configs.newtonian_grid(num_pupil=100))
     a = run_rayfunction(s, g).outputs.numpy()
     rin = O.input_rays(s, g["wavelength"], g["field_x"], g["field_y"], g["pupil_x"], g["pupil_y"])
     rays = ok.rays.RayVectorArray(
@@ -136,7 +146,10 @@ def _single_surface_rays(n=4000, seed=11, spread=0.15):
     pz = np.full(n, -100.0)
     dx, dy, dz = O.direction(rng.uniform(-spread, spread, n), rng.uniform(-spread, spread, n))
     wl = rng.uniform(400, 700, n)
-    return O.make_rays((n,), px=px, py=py, pz=pz, dx=dx, dy=dy, dz=dz, wavelength=wl)
+    r = O.make_rays((n,), px=px, py=py, pz=pz, dx=dx, dy=dy, dz=dz, wavelength=wl)
+    for k in ("px", "py", "pz", "dx", "dy", "dz", "wavelength"):
+        r[k] = r[k].astype(np.float32).astype(np.float64)
+    return r
 
 
 def _gpu_propagate(surfaces, r):
@@ -234,7 +247,7 @@ def test_rulings(cuda, kind):
         rulings=ok.rulings.Rulings(spacing=spacing, diffraction_order=1))
     det = ok.surfaces.Surface(transformation=ok.transforms.Translation(z=-500.0))
     r = _single_surface_rays(seed=17, spread=0.05)
-    r["wavelength"] = np.linspace(58, 63, r["px"].size)
+    r["wavelength"] = np.linspace(58, 63, r["px"].size).astype(np.float32).astype(np.float64)
     ref = O.propagate_rays([surface, det], r)
     out = _gpu_propagate([surface, det], r)
     m = ref["unvignetted"] & np.isfinite(ref["px"])
@@ -257,13 +270,13 @@ def test_multilayer_vs_imd_golden(cuda, name):
 def test_multilayer_periodic_vs_oracle(cuda):
     rng = np.random.default_rng(4)
     n = 20000
-    wl = rng.uniform(12, 15, n)
-    cos = np.cos(rng.uniform(0, 20 * math.pi / 180, n))
+    wl = rng.uniform(12, 15, n).astype(np.float32).astype(np.float64)
+    cos = np.cos(rng.uniform(0, 20 * math.pi / 180, n)).astype(np.float32).astype(np.float64)
     d = 10.0
-    A = ok.materials.Layer(1 - 0.02 + 0.004j, 0.4 * d)
-    B = ok.materials.Layer(1 - 0.002 + 0.0006j, 0.6 * d)
+    A = ok.materials.Layer(c32(1 - 0.02 + 0.004j), 0.4 * d)
+    B = ok.materials.Layer(c32(1 - 0.002 + 0.0006j), 0.6 * d)
     stack = ok.materials.PeriodicLayerSequence([A, B], num_periods=40)
-    sub = ok.materials.Layer(1 - 0.03 + 0.01j)
+    sub = ok.materials.Layer(c32(1 - 0.03 + 0.01j))
     R, T = ok.multilayer_efficiency(wl, cos, 1.0, stack, sub)
     Rs, Rp, Ts, Tp = O.multilayer_efficiency(wl, cos, 1.0, stack, sub)
     assert np.abs(R.s.cpu().numpy() - Rs).max() < 1e-5
@@ -275,11 +288,12 @@ def test_multilayer_periodic_vs_oracle(cuda):
 def test_multilayer_film_and_table_interp(cuda):
     rng = np.random.default_rng(8)
     n = 5000
-    chem = ok.chemicals.Chemical(wavelength=[10.0, 20.0, 35.0, 50.0], n=[0.9, 0.95, 0.97, 0.99],
-                                 k=[0.05, 0.02, 0.01, 0.004])
-    wl = rng.uniform(5, 60, n)  # includes clamped ends
-    cos = np.cos(rng.uniform(0, 1.0, n))
-    layers = [ok.materials.Layer(chem, 15.0), ok.materials.Layer(0.98 + 0.003j, 7.0)]
+    chem = ok.chemicals.Chemical(wavelength=[10.0, 20.0, 35.0, 50.0],
+                                 n=np.float32([0.9, 0.95, 0.97, 0.99]),
+                                 k=np.float32([0.05, 0.02, 0.01, 0.004]))
+    wl = rng.uniform(5, 60, n).astype(np.float32).astype(np.float64)  # includes clamped ends
+    cos = np.cos(rng.uniform(0, 1.0, n)).astype(np.float32).astype(np.float64)
+    layers = [ok.materials.Layer(chem, 15.0), ok.materials.Layer(c32(0.98 + 0.003j), 7.0)]
     R, T = ok.multilayer_efficiency(wl, cos, 1.0, layers, None)
     Rs, Rp, Ts, Tp = O.multilayer_efficiency(wl, cos, 1.0, layers, None)
     assert np.abs(T.average.cpu().numpy() - (Ts + Tp) / 2).max() < 1e-5
