@@ -111,6 +111,16 @@ typedef struct otx_stack {
   int32_t substrate; /* layer index, or -1 for vacuum */
 } otx_stack;
 
+/* One periodic bilayer mirror: [A, B] x num_periods on a substrate, with
+ * constant complex indices (optika/materials/_layers.py:571-645 with two
+ * layers of constant index). */
+typedef struct otx_periodic_stack {
+  float n_a_re, n_a_im, n_b_re, n_b_im, n_sub_re, n_sub_im;
+  float thickness_a, thickness_b; /* nm */
+  int32_t num_periods;
+  int32_t pad_;
+} otx_periodic_stack;
+
 typedef struct otx_table {
   int32_t offset; /* into otx_system.table_data: [wl(n), n(n), k(n)] */
   int32_t count;
@@ -217,6 +227,33 @@ typedef struct otx_image {
   uint64_t flux;   /* float   [num_w][num_x][num_y] or 0 */
 } otx_image;
 
+/* Batched trace of many configurations of one system shape.  Each config
+ * replaces num_overrides surfaces of the base system (at override_index)
+ * with its own descriptors; its rays are generated on the device by
+ * Philox4x32-10 keyed by (seed, config) and counted by ray index:
+ * wavelength U[wl_lo, wl_hi), field angles U[-half, half) in x and y,
+ * pupil U[-pupil_half, pupil_half)^2.  Work items are tiles of up to
+ * tile_size rays of one config, listed in `tiles`, taken by persistent CTAs
+ * from the device counter `counter` (a uint32 the entry point clears). */
+#define OTX_BATCH_MAX_OVERRIDES 4
+typedef struct otx_batch {
+  int32_t num_configs;
+  int32_t num_overrides;
+  int32_t override_index[OTX_BATCH_MAX_OVERRIDES];
+  int32_t tile_size;
+  int32_t pad_;
+  uint64_t overrides;  /* device otx_surface[num_configs][num_overrides]     */
+  uint64_t ray_offset; /* device int64[num_configs + 1], prefix sums         */
+  uint64_t tiles;      /* device int32[num_tiles][2]: config, first ray      */
+  int64_t num_tiles;
+  uint64_t counter;    /* device uint32 work counter (scratch)               */
+  uint64_t seed;
+  float wl_lo, wl_hi;
+  float field_x_half, field_y_half; /* rad */
+  float pupil_half;                 /* mm  */
+  int32_t image_stride;             /* elements between config images     */
+} otx_batch;
+
 typedef struct otx_launch {
   int32_t rays_per_thread; /* 1, 2 or 4; 0 = library default          */
   int32_t block_size;      /* threads per CTA; 0 = library default     */
@@ -228,7 +265,8 @@ typedef struct otx_launch {
 
 /* ABI self-description: sizes of the descriptor structs, for binding
  * checks.  `which`: 0 otx_system, 1 otx_surface, 2 otx_rays, 3 otx_grid,
- * 4 otx_image, 5 otx_launch, 6 otx_affine, 7 otx_sensor. */
+ * 4 otx_image, 5 otx_launch, 6 otx_affine, 7 otx_sensor, 8 otx_layer,
+ * 9 otx_stack, 10 otx_periodic_stack, 11 otx_batch. */
 int64_t otx_sizeof(int32_t which);
 int32_t otx_abi_version(void);
 const char* otx_status_string(otx_status s);
@@ -250,7 +288,8 @@ otx_status otx_trace_grid(const otx_system* sys, const otx_grid* in,
                           const otx_rays* out, const otx_image* image,
                           const otx_launch* launch, void* stream);
 
-/* Multilayer reflectivity / transmissivity of `count` samples.
+/* Multilayer reflectivity / transmissivity of `count` samples (float-float
+ * transfer matrices).
  * Replaces optika/materials/_multilayers.py:240-532 (multilayer_efficiency).
  * wavelength (nm), cos_incidence (direction), n_ambient (re, im) are float*
  * device arrays with strides (0 = broadcast); stack_index (int32*, may be
@@ -262,6 +301,30 @@ otx_status otx_multilayer_efficiency(
     const float* n_re, const float* n_im, int64_t stride_n,
     const int32_t* stack_index, float* r_s, float* r_p, float* t_s,
     float* t_p, void* stream);
+
+/* Trace every configuration of a batch in one persistent launch.
+ * Replaces optika's broadcasting of a SequentialSystem over configuration
+ * axes (optika/_util.py:21-38, shape of every component) in
+ * raytrace / rayfunction (optika/systems/_sequential.py:836-988).  Outputs
+ * (sensor frame) are indexed ray_offset[config] + ray; images, if given,
+ * are per config, image_stride elements apart. */
+otx_status otx_trace_batch(const otx_system* base, const otx_batch* batch,
+                           const otx_rays* out, const otx_image* image,
+                           const otx_launch* launch, void* stream);
+
+/* Reflectivity / transmissivity of `count` samples over a batch of
+ * periodic bilayer mirrors (float-float transfer matrices).  configs is a
+ * device array of num_configs entries, config_index (int32*, may be null =
+ * config 0) selects one per sample; wavelength (nm) and cos_incidence are
+ * float* device arrays with strides (0 = broadcast); the ambient index is
+ * n_re + i n_im.  Replaces optika/materials/_multilayers.py:240-532 for
+ * PeriodicLayerSequence stacks (optika/materials/_layers.py:611-645). */
+otx_status otx_multilayer_periodic(const otx_periodic_stack* configs, int32_t num_configs,
+                                   int64_t count, const float* wavelength,
+                                   int64_t stride_wavelength, const float* cos_incidence,
+                                   int64_t stride_cos, const int32_t* config_index,
+                                   float n_re, float n_im, float* r_s, float* r_p,
+                                   float* t_s, float* t_p, void* stream);
 
 /* Bin rays given in the sensor's local frame into count and flux images.
  * Replaces optika/sensors/_sensors.py:92-161 (ImagingSensor.collect, the

@@ -380,3 +380,39 @@ def multilayer_efficiency_gpu(wavelength, direction, n, layers, substrate):
     L.check(st, "otx_multilayer_efficiency")
     rs, rp, ts, tp = (o.reshape(shape) for o in outs)
     return PolarizationVectorArray(rs, rp), PolarizationVectorArray(ts, tp)
+
+
+def periodic_table(mirrors, dev) -> torch.Tensor:
+    """Pack PeriodicMirror descriptions into a device otx_periodic_stack array."""
+    arr = (L.PeriodicStack * len(mirrors))()
+    for i, m in enumerate(mirrors):
+        na, nb, ns = (complex(x.chemical) for x in (m.a, m.b, m.substrate))
+        d = arr[i]
+        d.n_a_re, d.n_a_im = na.real, na.imag
+        d.n_b_re, d.n_b_im = nb.real, nb.imag
+        d.n_sub_re, d.n_sub_im = ns.real, ns.imag
+        d.thickness_a, d.thickness_b = float(m.a.thickness), float(m.b.thickness)
+        d.num_periods = int(m.num_periods)
+    raw = bytes(arr)
+    return torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(dev)
+
+
+def multilayer_periodic_gpu(wavelength, direction, mirrors, index, n):
+    dev = device()
+    table = periodic_table(mirrors, dev)
+    fields, shape = _broadcast_inputs([wavelength, direction], dev)
+    cnt = int(np.prod(shape)) if len(shape) else 1
+    idx = None
+    if index is not None:
+        idx = torch.as_tensor(np.asarray(index) if not isinstance(index, torch.Tensor) else index,
+                              device=dev).to(torch.int32).expand(shape).reshape(-1).contiguous()
+    outs = [torch.empty(cnt, dtype=torch.float32, device=dev) for _ in range(4)]
+    n = complex(n)
+    lib = L.load()
+    st = lib.otx_multilayer_periodic(
+        ptr(table), len(mirrors), cnt, ptr(fields[0].t), fields[0].stride, ptr(fields[1].t),
+        fields[1].stride, ptr(idx), n.real, n.imag, *(ptr(o) for o in outs), stream_handle(),
+    )
+    L.check(st, "otx_multilayer_periodic")
+    rs, rp, ts, tp = (o.reshape(shape) for o in outs)
+    return PolarizationVectorArray(rs, rp), PolarizationVectorArray(ts, tp)

@@ -72,6 +72,21 @@ class Stack(ctypes.Structure):
     ]
 
 
+class PeriodicStack(ctypes.Structure):
+    _fields_ = [
+        ("n_a_re", f32),
+        ("n_a_im", f32),
+        ("n_b_re", f32),
+        ("n_b_im", f32),
+        ("n_sub_re", f32),
+        ("n_sub_im", f32),
+        ("thickness_a", f32),
+        ("thickness_b", f32),
+        ("num_periods", i32),
+        ("pad_", i32),
+    ]
+
+
 class Table(ctypes.Structure):
     _fields_ = [("offset", i32), ("count", i32)]
 
@@ -191,6 +206,28 @@ class Image(ctypes.Structure):
     _fields_ = [("counts", u64), ("flux", u64)]
 
 
+class Batch(ctypes.Structure):
+    _fields_ = [
+        ("num_configs", i32),
+        ("num_overrides", i32),
+        ("override_index", i32 * 4),
+        ("tile_size", i32),
+        ("pad_", i32),
+        ("overrides", u64),
+        ("ray_offset", u64),
+        ("tiles", u64),
+        ("num_tiles", i64),
+        ("counter", u64),
+        ("seed", u64),
+        ("wl_lo", f32),
+        ("wl_hi", f32),
+        ("field_x_half", f32),
+        ("field_y_half", f32),
+        ("pupil_half", f32),
+        ("image_stride", i32),
+    ]
+
+
 class Launch(ctypes.Structure):
     _fields_ = [
         ("rays_per_thread", i32),
@@ -211,6 +248,8 @@ LAYOUT = {
     7: Sensor,
     8: Layer,
     9: Stack,
+    10: PeriodicStack,
+    11: Batch,
 }
 
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "_lib" / "liboptika_gb300.so"
@@ -250,6 +289,12 @@ def _declare(lib: ctypes.CDLL) -> None:
         P(System), i64, v, i64, v, i64, v, v, i64, v, v, v, v, v, v,
     ]
     lib.otx_multilayer_efficiency.restype = i32
+    lib.otx_multilayer_periodic.argtypes = [
+        v, i32, i64, v, i64, v, i64, v, f32, f32, v, v, v, v, v,
+    ]
+    lib.otx_multilayer_periodic.restype = i32
+    lib.otx_trace_batch.argtypes = [P(System), P(Batch), P(Rays), P(Image), P(Launch), v]
+    lib.otx_trace_batch.restype = i32
     lib.otx_collect.argtypes = [P(Sensor), P(Rays), P(Image), v]
     lib.otx_collect.restype = i32
     lib.otx_sag_eval.argtypes = [P(System), i32, P(Rays), P(Rays), v]

@@ -113,3 +113,84 @@ def precision_grid(n: int, seed: int = 2) -> dict:
     px, py = annulus(rng, n)
     wl = rng.uniform(400.0, 700.0, n)
     return dict(wavelength=wl, field_x=fx, field_y=fy, pupil_x=px, pupil_y=py)
+
+
+# ---------------------------------------------------------------- spectrograph
+
+# Geometry of the batched EUV imaging spectrograph, fixed once: a spherical
+# primary (R -1600 mm, 40 mm aperture) at z = 1000 mm focuses the beam back
+# towards -z; a toroidal VLS grating 600 mm in front of it (concave to the
+# returning beam: minor radius 1150 mm, radius of rotation 1200 mm in its
+# own frame, light arriving along -z) re-images the spectrum onto a
+# 2048 x 1024 sensor of 13.5 um pixels at the grating's first-order focus
+# for 60.5 nm and 2400 lines/mm (147.5 mm along the 8.378 deg diffracted
+# chief ray, found with the float64 oracle).  The reference's toroid places
+# its vertex at the origin only for a non-negative radius of rotation
+# (z = r - sqrt((r - z_y)^2 - x^2)), hence the positive radii facing the
+# returning beam.
+SPEC_PRIMARY_Z = 1000.0
+SPEC_GRATING_Z = 400.0
+SPEC_SENSOR_X = 21.4613817
+SPEC_SENSOR_Z = 545.943704
+SPEC_SENSOR_ANGLE = 8.377987233014737 * DEG
+SPEC_FIELD_HALF = (0.01 * DEG, 0.05 * DEG)
+SPEC_PUPIL_HALF = 40.0
+SPEC_WAVELENGTH = (58.0, 63.0)
+
+
+def spectrograph(d0: float = 1 / 2400, a1: float = 0.0, a2: float = 0.0,
+                 tilt: float = 0.0) -> systems.SequentialSystem:
+    """One configuration: ruling spacing d(x) = d0 (1 + a1 x + a2 x^2) (mm)
+    along x, grating tilt (rad) about y, diffraction order +1."""
+    from . import rulings
+
+    primary = surfaces.Surface(
+        name="primary",
+        sag=sags.SphericalSag(-1600.0),
+        material=materials.Mirror(),
+        aperture=apertures.CircularAperture(40.0),
+        is_pupil_stop=True,
+        transformation=transforms.Translation(z=SPEC_PRIMARY_Z),
+    )
+    grating = surfaces.Surface(
+        name="grating",
+        sag=sags.ToroidalSag(radius=1150.0, radius_of_rotation=1200.0),
+        material=materials.Mirror(),
+        rulings=rulings.Rulings(
+            spacing=rulings.Polynomial1dRulingSpacing(
+                {0: d0, 1: d0 * a1, 2: d0 * a2}, normal=(1.0, 0.0, 0.0)
+            ),
+            diffraction_order=1,
+        ),
+        transformation=transforms.TransformationList(
+            [transforms.RotationY(tilt), transforms.Translation(z=SPEC_GRATING_Z)]
+        ),
+    )
+    sensor = sensors.ImagingSensor(
+        name="sensor",
+        width_pixel=0.0135,
+        num_pixel=(2048, 1024),
+        transformation=transforms.TransformationList(
+            [transforms.RotationY(SPEC_SENSOR_ANGLE),
+             transforms.Translation(x=SPEC_SENSOR_X, z=SPEC_SENSOR_Z)]
+        ),
+    )
+    return systems.SequentialSystem(
+        object=surfaces.Surface(name="object"), surfaces=[primary, grating], sensor=sensor
+    )
+
+
+def spectrograph_batch(num_configs: int = 4096, seed: int = 3, min_rays: int = 1000,
+                       max_rays: int = 1_000_000) -> tuple[list, np.ndarray, np.ndarray]:
+    """Seeded configurations: 1/d0 ~ U(2200, 2600) lines/mm, a1 ~ N(0, 1e-4),
+    a2 ~ N(0, 1e-7), tilt ~ U(-2, 2) deg; ray counts log-uniform in
+    [min_rays, max_rays].  Returns (systems, ray counts, parameters[c, 4])."""
+    rng = np.random.default_rng(seed)
+    d0 = 1.0 / rng.uniform(2200.0, 2600.0, num_configs)
+    a1 = rng.normal(0.0, 1e-4, num_configs)
+    a2 = rng.normal(0.0, 1e-7, num_configs)
+    tilt = rng.uniform(-2.0, 2.0, num_configs) * DEG
+    counts = np.floor(10 ** rng.uniform(np.log10(min_rays), np.log10(max_rays), num_configs))
+    params = np.stack([d0, a1, a2, tilt], axis=-1)
+    systems_ = [spectrograph(*p) for p in params]
+    return systems_, counts.astype(np.int64), params

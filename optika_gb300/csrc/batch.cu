@@ -1,0 +1,221 @@
+// Batched trace: many configurations of one system shape in one persistent
+// launch.
+//
+// Persistent CTAs take work items (a tile of up to tile_size rays of one
+// configuration) from a device counter.  A CTA keeps the surface
+// descriptors of its current configuration in shared memory (the base
+// system's surfaces, with the configuration's overridden surfaces copied
+// over them), generates its rays with Philox4x32-10 and traces them with the
+// same device functions as the single-system kernels.  Configurations with
+// uneven ray counts (1e3 .. 1e6) balance through the shared counter.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "../../include/optika_gb300.h"
+#include "philox.cuh"
+#include "trace_kernel.cuh"
+
+namespace otx {
+
+struct BatchArgs {
+  otx_batch b;
+  otx_rays out;
+  otx_image img;
+};
+
+// Rays of the batch: wavelength, field angles and pupil position from two
+// Philox blocks (counter: ray index, config, block), each value formed
+// with explicitly rounded FP32 operations so that the host restatement
+// reproduces it exactly.
+__device__ __forceinline__ void batch_ray(const otx_batch& b, int cfg, int64_t i, Ray& r) {
+  const uint32_t k0 = (uint32_t)b.seed, k1 = (uint32_t)(b.seed >> 32);
+  const u32x4 c0 = philox4x32_10(u32x4{(uint32_t)i, (uint32_t)(i >> 32), (uint32_t)cfg, 0u}, k0, k1);
+  const u32x4 c1 = philox4x32_10(u32x4{(uint32_t)i, (uint32_t)(i >> 32), (uint32_t)cfg, 1u}, k0, k1);
+  const float wl = __fadd_rn(b.wl_lo, __fmul_rn(u01(c0.x), __fsub_rn(b.wl_hi, b.wl_lo)));
+  const float fx = __fmul_rn(b.field_x_half, __fsub_rn(__fmul_rn(2.f, u01(c0.y)), 1.f));
+  const float fy = __fmul_rn(b.field_y_half, __fsub_rn(__fmul_rn(2.f, u01(c0.z)), 1.f));
+  const float qx = __fmul_rn(b.pupil_half, __fsub_rn(__fmul_rn(2.f, u01(c0.w)), 1.f));
+  const float qy = __fmul_rn(b.pupil_half, __fsub_rn(__fmul_rn(2.f, u01(c1.x)), 1.f));
+  r.px = qx;
+  r.py = qy;
+  r.pz = 0.f;
+  direction_from_angles(fx, fy, r.dx, r.dy, r.dz);
+  r.lx = r.ly = r.lz = 0.f;
+  r.wl = wl;
+  r.inten = 1.f;
+  r.att = 0.f;
+  r.n = 1.f;
+  r.ok = true;
+  r.opl_hi = 0.f;
+  r.opl_lo = 0.f;
+}
+
+template <int I, class K, class... Rest>
+__device__ __forceinline__ void propagate_smem(const otx_system& sys, const otx_surface* s,
+                                               Ray& r) {
+  propagate_surface<K, false>(sys, s[I], r);
+  if constexpr (sizeof...(Rest) > 0) propagate_smem<I + 1, Rest...>(sys, s, r);
+}
+
+template <class... Ks>
+__device__ __forceinline__ void propagate_all(const otx_system& sys, const otx_surface* s,
+                                              Ray& r) {
+  if constexpr (sizeof...(Ks) > 0) {
+    propagate_smem<0, Ks...>(sys, s, r);
+  } else {
+    for (int k = 0; k < sys.num_surfaces; ++k) propagate_surface<AnyKind, true>(sys, s[k], r);
+  }
+}
+
+template <int RPT, class... Ks>
+__global__ void __launch_bounds__(256) k_trace_batch(const __grid_constant__ otx_system sys,
+                                                     const __grid_constant__ BatchArgs a) {
+  __shared__ otx_surface surf[OTX_MAX_SURFACES];
+  __shared__ int s_item;
+  const otx_batch& b = a.b;
+  const int tid = threadIdx.x;
+  const int ns = sys.num_surfaces;
+  {
+    const int words = ns * (int)(sizeof(otx_surface) / 4);
+    const int* src = reinterpret_cast<const int*>(sys.surfaces);
+    int* dst = reinterpret_cast<int*>(surf);
+    for (int w = tid; w < words; w += blockDim.x) dst[w] = src[w];
+  }
+  const otx_surface* ov = reinterpret_cast<const otx_surface*>(b.overrides);
+  const int64_t* offs = reinterpret_cast<const int64_t*>(b.ray_offset);
+  const int32_t* tiles = reinterpret_cast<const int32_t*>(b.tiles);
+  unsigned int* counter = reinterpret_cast<unsigned int*>(b.counter);
+  const bool bin = (a.img.counts != 0) || (a.img.flux != 0);
+  int cur = -1;
+  for (;;) {
+    __syncthreads();  // previous item done: s_item and surf may be rewritten
+    if (tid == 0) s_item = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int item = s_item;
+    if ((int64_t)item >= b.num_tiles) break;
+    const int cfg = tiles[2 * item];
+    const int64_t start = tiles[2 * item + 1];
+    if (cfg < 0 || cfg >= b.num_configs) continue;
+    if (cfg != cur) {
+      const int words = (int)(sizeof(otx_surface) / 4);
+      for (int j = 0; j < b.num_overrides; ++j) {
+        const int* src = reinterpret_cast<const int*>(ov + (int64_t)cfg * b.num_overrides + j);
+        int* dst = reinterpret_cast<int*>(surf + b.override_index[j]);
+        for (int w = tid; w < words; w += blockDim.x) dst[w] = src[w];
+      }
+      __syncthreads();
+      cur = cfg;
+    }
+    const int64_t base = offs[cfg];
+    const int64_t n_c = offs[cfg + 1] - base;
+    const int64_t end = start + b.tile_size < n_c ? start + b.tile_size : n_c;
+    for (int64_t i0 = start + tid; i0 < end; i0 += (int64_t)blockDim.x * RPT) {
+      Ray r[RPT];
+#pragma unroll
+      for (int k = 0; k < RPT; ++k) {
+        const int64_t i = i0 + (int64_t)k * blockDim.x;
+        if (i < end) {
+          batch_ray(b, cfg, i, r[k]);
+          propagate_all<Ks...>(sys, surf, r[k]);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < RPT; ++k) {
+        const int64_t i = i0 + (int64_t)k * blockDim.x;
+        if (i < end) {
+          if (bin) {
+            otx_image img = a.img;
+            const int64_t off = (int64_t)cfg * b.image_stride;
+            if (img.counts) img.counts += off * 4;
+            if (img.flux) img.flux += off * 4;
+            bin_ray(sys.sensor, img, r[k]);
+          }
+          store_ray<true>(a.out, base + i, sys.final_to_output, r[k]);
+        }
+      }
+    }
+  }
+}
+
+using BObject = Kind<OTX_SAG_FLAT, OTX_MAT_VACUUM, OTX_APER_NONE, OTX_RULE_NONE>;
+using BSphere = Kind<OTX_SAG_SPHERE, OTX_MAT_MIRROR, OTX_APER_CIRCULAR, OTX_RULE_NONE>;
+using BGrating = Kind<OTX_SAG_TOROID, OTX_MAT_MIRROR, OTX_APER_NONE, OTX_RULE_POLY1D>;
+using BSensor = Kind<OTX_SAG_FLAT, OTX_MAT_VACUUM, OTX_APER_RECTANGULAR, OTX_RULE_NONE>;
+
+template <class... Ks>
+static void launch_batch(int rpt, int grid, int block, const otx_system& sys, const BatchArgs& a,
+                         cudaStream_t st) {
+  if (rpt == 2)
+    k_trace_batch<2, Ks...><<<grid, block, 0, st>>>(sys, a);
+  else
+    k_trace_batch<1, Ks...><<<grid, block, 0, st>>>(sys, a);
+}
+
+}  // namespace otx
+
+using namespace otx;
+
+extern "C" otx_status otx_trace_batch(const otx_system* base, const otx_batch* batch,
+                                      const otx_rays* out, const otx_image* image,
+                                      const otx_launch* launch, void* stream) {
+  if (!base || !batch || !out) return OTX_ERR_INVALID;
+  if (base->abi_version != OTX_ABI_VERSION) return OTX_ERR_INVALID;
+  if (base->num_surfaces < 1 || base->num_surfaces > OTX_MAX_SURFACES) return OTX_ERR_SIZE;
+  if (base->input_mode != OTX_INPUT_GRID_INFINITY) return OTX_ERR_INVALID;
+  const otx_batch& b = *batch;
+  if (b.num_configs < 0 || b.num_tiles < 0 || b.tile_size < 1) return OTX_ERR_INVALID;
+  if (b.num_overrides < 0 || b.num_overrides > OTX_BATCH_MAX_OVERRIDES) return OTX_ERR_SIZE;
+  for (int j = 0; j < b.num_overrides; ++j)
+    if (b.override_index[j] < 0 || b.override_index[j] >= base->num_surfaces)
+      return OTX_ERR_INVALID;
+  if (b.num_tiles == 0) return OTX_OK;
+  if (!b.ray_offset || !b.tiles || !b.counter || (b.num_overrides > 0 && !b.overrides))
+    return OTX_ERR_INVALID;
+  const bool bin = image && (image->counts || image->flux);
+  if (bin && (base->sensor.num_x < 1 || base->sensor.num_y < 1 || base->sensor.num_w < 1 ||
+              !(base->sensor.width_x > 0.f) || !(base->sensor.width_y > 0.f) ||
+              b.image_stride < base->sensor.num_w * base->sensor.num_x * base->sensor.num_y))
+    return OTX_ERR_INVALID;
+  int rpt = (launch && launch->rays_per_thread > 0) ? launch->rays_per_thread : 1;
+  if (rpt != 1 && rpt != 2) return OTX_ERR_INVALID;
+  int block = (launch && launch->block_size > 0) ? launch->block_size : 256;
+  if (block > 256 || block % 32 != 0) return OTX_ERR_INVALID;
+
+  otx_system sys = *base;
+  otx_sensor& S = sys.sensor;
+  S.inv_width_x = S.width_x > 0.f ? 1.f / S.width_x : 0.f;
+  S.inv_width_y = S.width_y > 0.f ? 1.f / S.width_y : 0.f;
+  S.inv_width_w = (S.w_hi > S.w_lo) ? (float)S.num_w / (S.w_hi - S.w_lo) : 0.f;
+  BatchArgs a;
+  memset(&a, 0, sizeof(a));
+  a.b = b;
+  a.out = *out;
+  if (bin) a.img = *image;
+
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (cudaMemsetAsync(reinterpret_cast<void*>(b.counter), 0, sizeof(unsigned int), st) !=
+      cudaSuccess)
+    return OTX_ERR_CUDA;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 132;
+  const int per_sm = 2048 / block;  // resident CTAs the scheduler can hold
+  int64_t grid = (int64_t)sms * (per_sm < 8 ? per_sm : 8);
+  if (grid > b.num_tiles) grid = b.num_tiles;
+
+  // the spectrograph shape (object, spherical mirror, toroidal VLS grating,
+  // sensor) runs its specialised kernel; anything else the generic one.
+  // Overridden surfaces keep the kinds of the base surfaces they replace
+  // (the host API checks this); the device functions bound every index
+  // they read from a descriptor, so a descriptor breaking it is wrong but
+  // never out of bounds.
+  const bool fixed =
+      !(launch && launch->generic_only) && shape_matches<BObject, BSphere, BGrating, BSensor>(sys);
+  if (fixed)
+    launch_batch<BObject, BSphere, BGrating, BSensor>(rpt, (int)grid, block, sys, a, st);
+  else
+    launch_batch<>(rpt, (int)grid, block, sys, a, st);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}

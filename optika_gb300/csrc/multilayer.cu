@@ -1,9 +1,10 @@
-// Standalone multilayer efficiency kernel (optika.materials.multilayer_efficiency).
+// Standalone multilayer efficiency kernels (optika.materials.multilayer_efficiency),
+// float-float transfer matrices.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "../../include/optika_gb300.h"
-#include "trace_device.cuh"
+#include "multilayer_ff.cuh"
 
 namespace otx {
 
@@ -20,7 +21,7 @@ struct MLArgs {
   float *rs, *rp, *ts, *tp;
 };
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128)
     k_multilayer(const __grid_constant__ otx_system sys, const __grid_constant__ MLArgs a) {
   const int64_t step = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count; i += step) {
@@ -29,13 +30,60 @@ __global__ void __launch_bounds__(256)
     const cf n0{a.n_re ? a.n_re[i * a.s_n] : 1.f, a.n_im ? a.n_im[i * a.s_n] : 0.f};
     int k = a.stack ? a.stack[i] : 0;
     k = (k < 0 || k >= OTX_MAX_STACKS) ? 0 : k;
+    const SysStackSource src{sys, sys.stacks[k]};
     float Rs, Rp, Ts, Tp;
-    multilayer(sys, sys.stacks[k], wl, c0, n0, Rs, Rp, Ts, Tp);
+    multilayer_pol_ff<true>(src, wl, c0, n0, false, Rs, Ts);
+    multilayer_pol_ff<true>(src, wl, c0, n0, true, Rp, Tp);
     if (a.rs) a.rs[i] = Rs;
     if (a.rp) a.rp[i] = Rp;
     if (a.ts) a.ts[i] = Ts;
     if (a.tp) a.tp[i] = Tp;
   }
+}
+
+struct PeriodicArgs {
+  const otx_periodic_stack* configs;
+  int32_t num_configs;
+  int64_t count;
+  const float* wl;
+  int64_t s_wl;
+  const float* cosv;
+  int64_t s_cos;
+  const int32_t* index;
+  float n_re, n_im;
+  float *rs, *rp, *ts, *tp;
+};
+
+// One thread per sample, both polarisations; the sample's mirror is read
+// from the config table (L1/L2 resident: 40 B per config).
+__global__ void __launch_bounds__(128) k_multilayer_periodic(const __grid_constant__ PeriodicArgs a) {
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  const cf n0{a.n_re, a.n_im};
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count; i += step) {
+    const float wl = a.wl[i * a.s_wl];
+    const float c0 = a.cosv[i * a.s_cos];
+    int k = a.index ? a.index[i] : 0;
+    k = (k < 0 || k >= a.num_configs) ? 0 : k;
+    const otx_periodic_stack P = a.configs[k];
+    const PeriodicSource src{P};
+    float Rs, Rp, Ts, Tp;
+    multilayer_pol_ff<true>(src, wl, c0, n0, false, Rs, Ts);
+    multilayer_pol_ff<true>(src, wl, c0, n0, true, Rp, Tp);
+    if (a.rs) a.rs[i] = Rs;
+    if (a.rp) a.rp[i] = Rp;
+    if (a.ts) a.ts[i] = Ts;
+    if (a.tp) a.tp[i] = Tp;
+  }
+}
+
+static int ml_grid(int64_t count, int block) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 132;
+  const int64_t need = (count + block - 1) / block;
+  const int64_t cap = (int64_t)sms * 32;
+  return (int)(need < cap ? need : cap);
 }
 
 }  // namespace otx
@@ -71,13 +119,23 @@ extern "C" otx_status otx_multilayer_efficiency(
   }
   MLArgs a{count, wavelength, stride_wavelength, cos_incidence, stride_cos, n_re, n_im,
            stride_n, stack_index, r_s, r_p, t_s, t_p};
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (sms <= 0) sms = 132;
-  int64_t need = (count + 255) / 256;
-  const int64_t cap = (int64_t)sms * 16;
-  const int grid = (int)(need < cap ? need : cap);
-  k_multilayer<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*sys, a);
+  k_multilayer<<<ml_grid(count, 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*sys, a);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+extern "C" otx_status otx_multilayer_periodic(const otx_periodic_stack* configs,
+                                              int32_t num_configs, int64_t count,
+                                              const float* wavelength, int64_t stride_wavelength,
+                                              const float* cos_incidence, int64_t stride_cos,
+                                              const int32_t* config_index, float n_re, float n_im,
+                                              float* r_s, float* r_p, float* t_s, float* t_p,
+                                              void* stream) {
+  if (count < 0 || num_configs < 0) return OTX_ERR_INVALID;
+  if (count == 0) return OTX_OK;
+  if (!configs || num_configs < 1 || !wavelength || !cos_incidence) return OTX_ERR_INVALID;
+  if (stride_wavelength < 0 || stride_cos < 0) return OTX_ERR_INVALID;
+  PeriodicArgs a{configs, num_configs, count, wavelength, stride_wavelength, cos_incidence,
+                 stride_cos, config_index, n_re, n_im, r_s, r_p, t_s, t_p};
+  k_multilayer_periodic<<<ml_grid(count, 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(a);
   return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
 }

@@ -1,0 +1,267 @@
+// Multilayer reflectivity / transmissivity in float-float arithmetic.
+//
+// Same formulation as the FP32 evaluator of trace_device.cuh (unnormalised
+// Yeh transfer matrices, optika/materials/_layers.py:229-277 and
+// optika/materials/_multilayers.py:187-237, 485-532), carried in
+// float-float: the period matrix of a periodic stack is raised to the power
+// N - 1, which multiplies its rounding error by ~N, so FP32 products and
+// FP32 phases leave T ~1e-5 off complex128 for 40 periods; float-float
+// keeps it ~1e-7.  The layer phases use float-float exp / sin / cos built
+// from argument reduction and Taylor series (no FP32 transcendental
+// enters the phase).
+#pragma once
+
+#include "ff.cuh"
+#include "trace_device.cuh"
+
+namespace otx {
+
+// 2 pi, pi / 2, ln 2 as float-float constants (hi + lo).
+__device__ __forceinline__ ff ff_2pi() { return ff{6.28318548202514648f, -1.74845553e-07f}; }
+__device__ __forceinline__ ff ff_pio2() { return ff{1.57079637050628662f, -4.37113883e-08f}; }
+__device__ __forceinline__ ff ff_ln2() { return ff{0.693147182464599609f, -1.90465421e-09f}; }
+
+// exp(x) for a float-float x: x = k ln2 + r, |r| <= ln2 / 2, exp(r) by its
+// Taylor series to r^13 / 13!, then scaled by 2^k.
+__device__ __forceinline__ ff ff_exp(ff x) {
+  if (x.hi > 88.f) return ff{INFINITY, 0.f};
+  if (x.hi < -103.f) return ff{0.f, 0.f};
+  const float k = rintf(x.hi * 1.44269504088896341f);
+  const ff r = ff_sub(x, ff_mulf(ff_ln2(), k));
+  ff term = ff_of(1.f), sum = ff_of(1.f);
+#pragma unroll
+  for (int i = 1; i <= 13; ++i) {
+    term = ff_div(ff_mul(term, r), ff_of((float)i));  // r^i / i!
+    sum = ff_add(sum, term);
+  }
+  return ff_scale2(sum, ldexpf(1.f, (int)k));
+}
+
+// sin and cos of a float-float x: x = k pi/2 + r, |r| <= pi/4, Taylor
+// series of sin(r), cos(r) to r^17, then the quadrant of k.
+__device__ __forceinline__ void ff_sincos(ff x, ff& s, ff& c) {
+  const float k = rintf(x.hi * 0.636619772367581343f);
+  const ff r = ff_sub(x, ff_mulf(ff_pio2(), k));
+  const ff r2 = ff_mul(r, r);
+  // sin r = r (1 - r^2/(2*3) (1 - r^2/(4*5) (1 - ...)))  (Horner on the ratios)
+  ff ps = ff_of(1.f), pc = ff_of(1.f);
+#pragma unroll
+  for (int i = 8; i >= 1; --i) {
+    const ff rs = ff_div(r2, ff_of((float)((2 * i) * (2 * i + 1))));
+    const ff rc = ff_div(r2, ff_of((float)((2 * i - 1) * (2 * i))));
+    ps = ff_sub(ff_of(1.f), ff_mul(rs, ps));
+    pc = ff_sub(ff_of(1.f), ff_mul(rc, pc));
+  }
+  const ff sr = ff_mul(r, ps);
+  const ff cr = pc;
+  const int q = ((int)k) & 3;
+  switch (q) {
+    case 0: s = sr; c = cr; break;
+    case 1: s = cr; c = ff_neg(sr); break;
+    case 2: s = ff_neg(sr); c = ff_neg(cr); break;
+    default: s = ff_neg(cr); c = sr; break;
+  }
+}
+
+// Transfer-matrix state of one polarisation (see MLState in
+// trace_device.cuh): unnormalised product with its exponent and, for T,
+// the product of |2 q_i|^2.
+struct MLff {
+  cmff m;
+  int e;
+  bool first;
+  ff t;
+  int te;
+  cff q;
+  cff inv0;
+  bool where;
+};
+
+__device__ __forceinline__ cff medium_q_ff(const cff& inv0, cf nj_f, bool pol_p) {
+  const cff nj = cff_of(nj_f.re, nj_f.im);
+  const cff nj2 = cff_mul(nj, nj);
+  const cff ratio = cff_div(inv0, nj2);
+  const cff cj = cff_sqrt(cff_sub(cff_of(1.f, 0.f), ratio));
+  const cff w = cff_mul(nj, cj);
+  if (!pol_p) return w;
+  return cff_scale(cff_conj(w), ff_div(ff_of(1.f), cff_abs2(nj)));
+}
+
+__device__ __forceinline__ void mlff_times(MLff& st, const cmff& t, int te) {
+  if (st.first) {
+    st.m = t;
+    st.e = te;
+    st.first = false;
+  } else {
+    st.m = cmff_mul(st.m, t);
+    st.e += te;
+  }
+  cmff_normalize(st.m, st.e);
+}
+
+__device__ __forceinline__ void ff_normalize_scalar(ff& t, int& te) {
+  if (!(t.hi > 0.f) || !isfinite(t.hi)) return;
+  const int e = ilogbf(t.hi);
+  t = ff_scale2(t, ldexpf(1.f, -e));
+  te += e;
+}
+
+template <bool NEED_T>
+__device__ __forceinline__ void layer_step_ff(MLff& st, cf nj, float thickness, float wl,
+                                              bool pol_p) {
+  const cff qj = medium_q_ff(st.inv0, nj, pol_p);
+  const cff a = cff_add(st.q, qj), b = cff_sub(st.q, qj);
+  bool wprop = true;
+  cmff tm{a, b, b, a};
+  if (thickness != 0.f) {
+    // beta = 2 pi h (n cos) / lambda ; n cos = q_s, or conj(q_p) |n|^2
+    cff ncos = qj;
+    if (pol_p) {
+      const cff njc = cff_of(nj.re, nj.im);
+      ncos = cff_scale(cff_conj(qj), cff_abs2(njc));
+    }
+    const ff k = ff_div(ff_mulf(ff_2pi(), thickness), ff_of(wl));
+    const cff beta = cff_scale(ncos, k);
+    ff sn, cs;
+    ff_sincos(beta.re, sn, cs);
+    const ff g = ff_exp(beta.im);  // |exp(-i beta)|
+    wprop = g.hi < 1e10f;
+    if (wprop) {
+      const ff gi = ff_div(ff_of(1.f), g);
+      const cff em{ff_mul(g, cs), ff_neg(ff_mul(g, sn))};
+      const cff ep{ff_mul(gi, cs), ff_mul(gi, sn)};
+      tm = cmff{cff_mul(a, em), cff_mul(b, ep), cff_mul(b, em), cff_mul(a, ep)};
+    }
+  }
+  if (st.where) {
+    mlff_times(st, tm, 0);
+    if (NEED_T) {
+      st.t = ff_mul(st.t, ff_scale2(cff_abs2(st.q), 4.f));
+      ff_normalize_scalar(st.t, st.te);
+    }
+  }
+  st.where = st.where && wprop;
+  st.q = qj;
+}
+
+__device__ __forceinline__ void cmff_pow(cmff base, int bexp, int e, cmff& acc, int& aexp) {
+  bool first = true;
+  while (e > 0) {
+    if (e & 1) {
+      if (first) {
+        acc = base;
+        aexp = bexp;
+        first = false;
+      } else {
+        acc = cmff_mul(acc, base);
+        aexp += bexp;
+        cmff_normalize(acc, aexp);
+      }
+    }
+    e >>= 1;
+    if (e) {
+      base = cmff_mul(base, base);
+      bexp *= 2;
+      cmff_normalize(base, bexp);
+    }
+  }
+}
+
+// A stack as seen by the evaluator: pre layers, a periodic block, post
+// layers and a substrate, each layer an index (at this wavelength) and a
+// thickness.
+struct SysStackSource {
+  const otx_system& sys;
+  const otx_stack& K;
+  __device__ int count(int section) const {
+    return section == 0 ? K.pre_count : (section == 1 ? K.per_count : K.post_count);
+  }
+  __device__ int periods() const { return K.num_periods; }
+  __device__ const otx_layer& lay(int section, int i) const {
+    const int b = section == 0 ? K.pre_begin : (section == 1 ? K.per_begin : K.post_begin);
+    return sys.layers[b + i];
+  }
+  __device__ cf n(int section, int i, float wl) const { return layer_n(sys, lay(section, i), wl); }
+  __device__ float h(int section, int i) const { return lay(section, i).thickness; }
+  __device__ cf n_sub(float wl) const {
+    return K.substrate >= 0 ? layer_n(sys, sys.layers[K.substrate], wl) : cf{1.f, 0.f};
+  }
+};
+
+struct PeriodicSource {
+  const otx_periodic_stack& P;
+  __device__ int count(int section) const { return section == 1 ? 2 : 0; }
+  __device__ int periods() const { return P.num_periods; }
+  __device__ cf n(int, int i, float) const {
+    return i == 0 ? cf{P.n_a_re, P.n_a_im} : cf{P.n_b_re, P.n_b_im};
+  }
+  __device__ float h(int, int i) const { return i == 0 ? P.thickness_a : P.thickness_b; }
+  __device__ cf n_sub(float) const { return cf{P.n_sub_re, P.n_sub_im}; }
+};
+
+template <bool NEED_T, class S>
+__device__ __forceinline__ void run_section_ff(MLff& st, const S& src, int section, float wl,
+                                               bool pol_p) {
+  const int n = src.count(section);
+  for (int i = 0; i < n; ++i) layer_step_ff<NEED_T>(st, src.n(section, i, wl), src.h(section, i), wl, pol_p);
+}
+
+// Reflectivity and transmissivity of one polarisation (float-float), the
+// same algorithm as multilayer_pol in trace_device.cuh.
+template <bool NEED_T, class S>
+__device__ __forceinline__ void multilayer_pol_ff(const S& src, float wl, float cos0, cf n0,
+                                                  bool pol_p, float& R, float& T) {
+  MLff st;
+  st.e = 0;
+  st.first = true;
+  st.t = ff_of(1.f);
+  st.te = 0;
+  const cff n0c = cff_of(n0.re, n0.im);
+  // (n0 sin0)^2 = n0^2 (1 - cos0^2)
+  const ff one_m_c2 = ff_sub(ff_of(1.f), ff_mul(ff_of(cos0), ff_of(cos0)));
+  st.inv0 = cff_scale(cff_mul(n0c, n0c), one_m_c2);
+  if (pol_p)
+    st.q = cff_scale(cff_conj(n0c), ff_div(ff_of(cos0), cff_abs2(n0c)));
+  else
+    st.q = cff_scale(n0c, ff_of(cos0));
+  const cff q0 = st.q;
+  st.where = true;
+  run_section_ff<NEED_T>(st, src, 0, wl, pol_p);
+  if (src.count(1) > 0 && src.periods() > 0) {
+    run_section_ff<NEED_T>(st, src, 1, wl, pol_p);  // first period
+    MLff per = st;
+    per.first = true;
+    per.e = 0;
+    per.t = ff_of(1.f);
+    per.te = 0;
+    run_section_ff<NEED_T>(per, src, 1, wl, pol_p);  // period from its own last medium
+    const int reps = src.periods() - 1;
+    if (!per.first && reps > 0) {
+      cmff pm;
+      int pe = 0;
+      cmff_pow(per.m, per.e, reps, pm, pe);
+      mlff_times(st, pm, pe);
+      if (NEED_T) {
+        for (int i = 0; i < reps; ++i) {
+          st.t = ff_mul(st.t, per.t);
+          st.te += per.te;
+          ff_normalize_scalar(st.t, st.te);
+        }
+      }
+    }
+    st.where = per.where;
+    st.q = per.q;
+  }
+  run_section_ff<NEED_T>(st, src, 2, wl, pol_p);
+  layer_step_ff<NEED_T>(st, src.n_sub(wl), 0.f, wl, pol_p);
+  const ff m11 = cff_abs2(st.m.a);
+  R = ff_to_f(ff_div(cff_abs2(st.m.c), m11));
+  T = 0.f;
+  if (NEED_T && st.where) {
+    const ff ratio = cff_div(st.q, q0).re;
+    const ff tt = ff_mul(ff_div(st.t, m11), ratio);
+    T = ldexpf(ff_to_f(tt), st.te - 2 * st.e);
+  }
+}
+
+}  // namespace otx

@@ -143,6 +143,8 @@ int64_t otx_sizeof(int32_t which) {
     case 7: return sizeof(otx_sensor);
     case 8: return sizeof(otx_layer);
     case 9: return sizeof(otx_stack);
+    case 10: return sizeof(otx_periodic_stack);
+    case 11: return sizeof(otx_batch);
     default: return -1;
   }
 }

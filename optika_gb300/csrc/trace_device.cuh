@@ -565,7 +565,8 @@ __device__ __forceinline__ void ruling_kappa(int rule_type, const otx_surface& s
       const float xs = fmaf(px, s.rule_normal[0],
                             fmaf(py, s.rule_normal[1], pz * s.rule_normal[2]));
       float d = 0.f;  // Horner over the dense coefficient table
-      for (int k = s.rule_num_terms - 1; k >= 0; --k) d = fmaf(d, xs, s.rule_coef[k]);
+      const int nt = min(max(s.rule_num_terms, 0), OTX_MAX_POLY_TERMS);
+      for (int k = nt - 1; k >= 0; --k) d = fmaf(d, xs, s.rule_coef[k]);
       kx = d * s.rule_normal[0];
       ky = d * s.rule_normal[1];
       kz = d * s.rule_normal[2];
@@ -652,7 +653,11 @@ __device__ __forceinline__ bool aperture_inside(int aper_type, const otx_system&
     case OTX_APER_POLYGON: {
       // even-odd crossing test over the vertex loop
       bool inside = false;
-      const int b = s.aper_vertex_begin, cnt = s.aper_vertex_count;
+      const int b = s.aper_vertex_begin;
+      const int cnt = (b >= 0 && s.aper_vertex_count >= 3 &&
+                       b + s.aper_vertex_count <= OTX_MAX_VERTICES)
+                          ? s.aper_vertex_count
+                          : 0;
       for (int i = 0, j = cnt - 1; i < cnt; j = i++) {
         const float xi = sys.vertices[2 * (b + i)], yi = sys.vertices[2 * (b + i) + 1];
         const float xj = sys.vertices[2 * (b + j)], yj = sys.vertices[2 * (b + j) + 1];
@@ -1058,9 +1063,10 @@ __device__ __forceinline__ void propagate_surface(const otx_system& sys,
       // n = n_ray + i att lambda / (4 pi), cos = -a.n (_multilayers.py:924-932)
       const float k = r.att * (r.wl * 1e-6f) * 0.07957747154594767f;
       const float cos0 = -(r.dx * nx + r.dy * ny + r.dz * nz);
-      const otx_stack& K2 = sys.stacks[s.mat_stack];
+      const int ks = min(max(s.mat_stack, 0), OTX_MAX_STACKS - 1);
+      const otx_stack& K2 = sys.stacks[ks];
       if (mat_type != OTX_MAT_FRESNEL_MIRROR && ML && stack_has_layers(K2))
-        eff = multilayer_efficiency_call(sys, s.mat_stack, mirror, r.wl, cos0, n1, k);
+        eff = multilayer_efficiency_call(sys, ks, mirror, r.wl, cos0, n1, k);
       else
         eff = fresnel_efficiency(sys, K2, mirror, r.wl, cos0, cf{n1, k});
       break;

@@ -30,6 +30,8 @@ __all__ = [
     "MultilayerMirror",
     "MultilayerFilm",
     "multilayer_efficiency",
+    "PeriodicMirror",
+    "multilayer_efficiency_periodic",
 ]
 
 
@@ -147,3 +149,32 @@ def multilayer_efficiency(
     from ._api import multilayer_efficiency_gpu
 
     return multilayer_efficiency_gpu(wavelength, direction, n, layers, substrate)
+
+
+@dataclasses.dataclass(eq=False)
+class PeriodicMirror:
+    """A periodic bilayer mirror ``[a, b] x num_periods`` on ``substrate``,
+    every medium of constant complex index (optika/materials/_layers.py:
+    571-645 with two layers)."""
+
+    a: Layer
+    b: Layer
+    num_periods: int
+    substrate: Layer
+
+    @property
+    def layers(self) -> PeriodicLayerSequence:
+        return PeriodicLayerSequence([self.a, self.b], self.num_periods)
+
+
+def multilayer_efficiency_periodic(wavelength, direction, mirrors, index=None, n=1.0):
+    """Batched :func:`multilayer_efficiency` over periodic bilayer mirrors.
+
+    ``mirrors`` is a sequence of :class:`PeriodicMirror`; ``index`` (int
+    array, or ``None`` for mirror 0) picks each sample's mirror.  Returns
+    ``(R, T)`` as :class:`~optika_gb300.vectors.PolarizationVectorArray` of
+    float32 CUDA tensors.  Transfer matrices are float-float.
+    """
+    from ._api import multilayer_periodic_gpu
+
+    return multilayer_periodic_gpu(wavelength, direction, mirrors, index, n)
