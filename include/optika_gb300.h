@@ -312,6 +312,26 @@ otx_status otx_trace_batch(const otx_system* base, const otx_batch* batch,
                            const otx_rays* out, const otx_image* image,
                            const otx_launch* launch, void* stream);
 
+/* otx_trace_batch without any allocation by the caller or the library.
+ *
+ * No counterpart in the reference.  For callers that cannot allocate GPU
+ * memory at the point of the call: a host application embedding this
+ * library whose device memory belongs to its own allocator, or code that
+ * may not allocate (allocation synchronises the device).  They pass only
+ * the inputs and outputs of otx_trace_batch; batch->tiles and
+ * batch->counter are ignored, batch->num_tiles must equal
+ * sum over configs of ceil(rays / tile_size) and may not exceed
+ * OTX_NOALLOC_MAX_TILES (larger batches return OTX_ERR_SIZE).  The work
+ * counter and the tile list live in a file-scope device array of the
+ * library (1 MiB, held by every GPU that loads the library until exit); the
+ * first call on a device looks up its address, so make it before any stream
+ * capture.  Every call shares that array and keeps the last call's
+ * contents: calls that overlap on the GPU (on concurrent streams) race. */
+#define OTX_NOALLOC_MAX_TILES 131000
+otx_status otx_trace_batch_noalloc(const otx_system* base, const otx_batch* batch,
+                                   const otx_rays* out, const otx_image* image,
+                                   const otx_launch* launch, void* stream);
+
 /* Reflectivity / transmissivity of `count` samples over a batch of
  * periodic bilayer mirrors (float-float transfer matrices).  configs is a
  * device array of num_configs entries, config_index (int32*, may be null =

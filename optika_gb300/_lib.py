@@ -16,6 +16,7 @@ MAX_POLY_TERMS = 8
 MAX_VERTICES = 64
 MAX_LAYERS = 64
 MAX_STACKS = 4
+NOALLOC_MAX_TILES = 131000
 
 OK = 0
 ERR_INVALID = 1
@@ -295,6 +296,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_multilayer_periodic.restype = i32
     lib.otx_trace_batch.argtypes = [P(System), P(Batch), P(Rays), P(Image), P(Launch), v]
     lib.otx_trace_batch.restype = i32
+    lib.otx_trace_batch_noalloc.argtypes = [P(System), P(Batch), P(Rays), P(Image), P(Launch), v]
+    lib.otx_trace_batch_noalloc.restype = i32
     lib.otx_collect.argtypes = [P(Sensor), P(Rays), P(Image), v]
     lib.otx_collect.restype = i32
     lib.otx_sag_eval.argtypes = [P(System), i32, P(Rays), P(Rays), v]

@@ -12,6 +12,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <mutex>
+
 #include "../../include/optika_gb300.h"
 #include "philox.cuh"
 #include "trace_kernel.cuh"
@@ -211,6 +213,145 @@ extern "C" otx_status otx_trace_batch(const otx_system* base, const otx_batch* b
   // (the host API checks this); the device functions bound every index
   // they read from a descriptor, so a descriptor breaking it is wrong but
   // never out of bounds.
+  const bool fixed =
+      !(launch && launch->generic_only) && shape_matches<BObject, BSphere, BGrating, BSensor>(sys);
+  if (fixed)
+    launch_batch<BObject, BSphere, BGrating, BSensor>(rpt, (int)grid, block, sys, a, st);
+  else
+    launch_batch<>(rpt, (int)grid, block, sys, a, st);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------- no allocation
+
+// Scratch of otx_trace_batch_noalloc: word 0 is the work counter, words
+// 64.. hold the tile list (config, first ray) of up to OTX_NOALLOC_MAX_TILES
+// work items.  It is a file-scope device array, so the entry point needs no
+// allocation; every GPU that loads the library holds its 1 MiB until exit,
+// and every call shares it.
+#define OTX_NOALLOC_HEADER_WORDS 64
+static __device__ __align__(256) int32_t g_noalloc_scratch[OTX_NOALLOC_HEADER_WORDS +
+                                                           2 * OTX_NOALLOC_MAX_TILES];
+
+namespace otx {
+
+// Tile list of a batch, built on the device from the ray-count prefix sums:
+// one CTA, each thread owning a contiguous run of configurations, a block
+// scan of their tile counts, then every thread writing its tiles.  Writes
+// are bounded by num_tiles; entries the prefix sums leave unwritten carry
+// config -1, which the trace kernel skips.
+__global__ void __launch_bounds__(1024) k_make_tiles(const int64_t* __restrict__ offs,
+                                                    int num_configs, int tile_size,
+                                                    int64_t num_tiles, int32_t* __restrict__ tiles) {
+  __shared__ int64_t sums[1024];
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int per = (num_configs + nt - 1) / nt;
+  const int c0 = tid * per, c1 = min(num_configs, c0 + per);
+  int64_t mine = 0;
+  for (int c = c0; c < c1; ++c) {
+    const int64_t n = offs[c + 1] - offs[c];
+    mine += n > 0 ? (n + tile_size - 1) / tile_size : 0;
+  }
+  sums[tid] = mine;
+  __syncthreads();
+  for (int d = 1; d < nt; d <<= 1) {  // inclusive Hillis-Steele scan
+    const int64_t v = tid >= d ? sums[tid - d] : 0;
+    __syncthreads();
+    sums[tid] += v;
+    __syncthreads();
+  }
+  int64_t t = sums[tid] - mine;  // exclusive prefix
+  for (int c = c0; c < c1; ++c) {
+    const int64_t n = offs[c + 1] - offs[c];
+    for (int64_t start = 0; start < n && t < num_tiles; start += tile_size, ++t) {
+      tiles[2 * t] = c;
+      tiles[2 * t + 1] = (int32_t)start;
+    }
+  }
+  const int64_t total = sums[nt - 1];
+  for (int64_t k = total + tid; k < num_tiles; k += nt) {
+    tiles[2 * k] = -1;
+    tiles[2 * k + 1] = 0;
+  }
+}
+
+static std::mutex g_noalloc_mutex;
+static int32_t* g_noalloc_ptr[64];
+
+// Device address of the scratch array for the current device, resolved
+// once per device (with that device current) by cudaGetSymbolAddress.
+static int32_t* noalloc_scratch(int dev) {
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return nullptr;
+    g_noalloc_ptr[dev] = static_cast<int32_t*>(p);
+  }
+  return g_noalloc_ptr[dev];
+}
+
+}  // namespace otx
+
+extern "C" otx_status otx_trace_batch_noalloc(const otx_system* base, const otx_batch* batch,
+                                              const otx_rays* out, const otx_image* image,
+                                              const otx_launch* launch, void* stream) {
+  if (!base || !batch || !out) return OTX_ERR_INVALID;
+  if (base->abi_version != OTX_ABI_VERSION) return OTX_ERR_INVALID;
+  if (base->num_surfaces < 1 || base->num_surfaces > OTX_MAX_SURFACES) return OTX_ERR_SIZE;
+  if (base->input_mode != OTX_INPUT_GRID_INFINITY) return OTX_ERR_INVALID;
+  const otx_batch& b = *batch;
+  if (b.num_configs < 0 || b.num_tiles < 0 || b.tile_size < 1) return OTX_ERR_INVALID;
+  if (b.num_tiles > OTX_NOALLOC_MAX_TILES) return OTX_ERR_SIZE;
+  if (b.num_overrides < 0 || b.num_overrides > OTX_BATCH_MAX_OVERRIDES) return OTX_ERR_SIZE;
+  for (int j = 0; j < b.num_overrides; ++j)
+    if (b.override_index[j] < 0 || b.override_index[j] >= base->num_surfaces)
+      return OTX_ERR_INVALID;
+  if (b.num_tiles == 0) return OTX_OK;
+  if (b.num_configs < 1 || !b.ray_offset || (b.num_overrides > 0 && !b.overrides))
+    return OTX_ERR_INVALID;
+  const bool bin = image && (image->counts || image->flux);
+  if (bin && (base->sensor.num_x < 1 || base->sensor.num_y < 1 || base->sensor.num_w < 1 ||
+              !(base->sensor.width_x > 0.f) || !(base->sensor.width_y > 0.f) ||
+              b.image_stride < base->sensor.num_w * base->sensor.num_x * base->sensor.num_y))
+    return OTX_ERR_INVALID;
+  int rpt = (launch && launch->rays_per_thread > 0) ? launch->rays_per_thread : 1;
+  if (rpt != 1 && rpt != 2) return OTX_ERR_INVALID;
+  int block = (launch && launch->block_size > 0) ? launch->block_size : 256;
+  if (block > 256 || block % 32 != 0) return OTX_ERR_INVALID;
+
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return OTX_ERR_CUDA;
+  int32_t* scratch = noalloc_scratch(dev);
+  if (!scratch) return OTX_ERR_CUDA;
+  int32_t* counter = scratch;
+  int32_t* tiles = scratch + OTX_NOALLOC_HEADER_WORDS;
+
+  otx_system sys = *base;
+  otx_sensor& S = sys.sensor;
+  S.inv_width_x = S.width_x > 0.f ? 1.f / S.width_x : 0.f;
+  S.inv_width_y = S.width_y > 0.f ? 1.f / S.width_y : 0.f;
+  S.inv_width_w = (S.w_hi > S.w_lo) ? (float)S.num_w / (S.w_hi - S.w_lo) : 0.f;
+  BatchArgs a;
+  memset(&a, 0, sizeof(a));
+  a.b = b;
+  a.b.tiles = reinterpret_cast<uint64_t>(tiles);
+  a.b.counter = reinterpret_cast<uint64_t>(counter);
+  a.out = *out;
+  if (bin) a.img = *image;
+
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  // the array keeps the previous call's contents: clear the counter
+  if (cudaMemsetAsync(counter, 0, OTX_NOALLOC_HEADER_WORDS * sizeof(int32_t), st) != cudaSuccess)
+    return OTX_ERR_CUDA;
+  k_make_tiles<<<1, 1024, 0, st>>>(reinterpret_cast<const int64_t*>(b.ray_offset), b.num_configs,
+                                   b.tile_size, b.num_tiles, tiles);
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 132;
+  const int per_sm = 2048 / block;
+  int64_t grid = (int64_t)sms * (per_sm < 8 ? per_sm : 8);
+  if (grid > b.num_tiles) grid = b.num_tiles;
   const bool fixed =
       !(launch && launch->generic_only) && shape_matches<BObject, BSphere, BGrating, BSensor>(sys);
   if (fixed)
