@@ -346,6 +346,36 @@ otx_status otx_multilayer_periodic(const otx_periodic_stack* configs, int32_t nu
                                    float n_re, float n_im, float* r_s, float* r_p,
                                    float* t_s, float* t_p, void* stream);
 
+/* ---- learned surrogate (BF16 MLP on tensor cores) ------------------- */
+/* No counterpart in the reference: the surrogate of the ray map is new.   */
+
+#define OTX_EPI_SILU_BF16 0 /* out = bf16(silu(A B^T + bias)), z = bf16(pre) */
+#define OTX_EPI_BIAS_F32 1  /* out = f32(A B^T + bias)                       */
+#define OTX_EPI_F32 2       /* out = f32(A B^T)                              */
+
+/* C[m x n] = epilogue(A B^T + bias): A bf16 [m x k] and B bf16 [n x k],
+ * row-major with row pitches lda, ldb (elements, multiples of 8, rows
+ * 16-byte aligned); tcgen05 tensor cores, TMA tiles, FP32 accumulation.
+ * n <= 256.  *err (device int) is set if a bounded wait gave up. */
+otx_status otx_gemm_bf16(const void* a, int32_t lda, const void* b, int32_t ldb, int32_t m,
+                         int32_t n, int32_t k, const float* bias, int32_t epilogue, void* out,
+                         int32_t ldo, void* z, int32_t* err, void* stream);
+/* dz = dy * silu'(z) (dy fp32, z and dz bf16, count elements). */
+otx_status otx_silu_backward(const float* dy, const void* z, void* dz, int64_t count,
+                             void* stream);
+/* out[c][r] = in[r][c] for a bf16 rows x cols matrix. */
+otx_status otx_transpose_bf16(const void* in, int32_t rows, int32_t cols, int32_t ldi, void* out,
+                              int32_t ldo, void* stream);
+/* out[c] = sum over rows of in[r][c] (bf16 in, fp32 out). */
+otx_status otx_colsum_bf16(const void* in, int32_t rows, int32_t cols, int32_t ldi, float* out,
+                           void* stream);
+/* One Adam step on fp32 master weights w (rows x cols) with moments m, v;
+ * writes bf16 copies w16 (row pitch ld16) and, if given, the transpose
+ * w16t (row pitch ld16t). */
+otx_status otx_adam(float* w, float* m, float* v, const float* grad, int32_t rows, int32_t cols,
+                    float lr, float beta1, float beta2, float eps, int32_t step, void* w16,
+                    int32_t ld16, void* w16t, int32_t ld16t, void* stream);
+
 /* Bin rays given in the sensor's local frame into count and flux images.
  * Replaces optika/sensors/_sensors.py:92-161 (ImagingSensor.collect, the
  * intensity-weighted na.histogram of position.xy and wavelength).  Reads

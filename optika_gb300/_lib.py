@@ -34,6 +34,7 @@ APER_FLAG_DIRECTION = 4
 APER_FLAG_TRANSFORM = 8
 RULE_NONE, RULE_CONSTANT, RULE_POLY1D, RULE_HOLOGRAPHIC = range(4)
 INPUT_RAYS, INPUT_GRID_INFINITY, INPUT_GRID_FINITE = range(3)
+EPI_SILU_BF16, EPI_BIAS_F32, EPI_F32 = range(3)
 SYS_FLAG_FINAL_IDENTITY = 1
 
 f32 = ctypes.c_float
@@ -298,6 +299,16 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_trace_batch.restype = i32
     lib.otx_trace_batch_noalloc.argtypes = [P(System), P(Batch), P(Rays), P(Image), P(Launch), v]
     lib.otx_trace_batch_noalloc.restype = i32
+    lib.otx_gemm_bf16.argtypes = [v, i32, v, i32, i32, i32, i32, v, i32, v, i32, v, v, v]
+    lib.otx_gemm_bf16.restype = i32
+    lib.otx_silu_backward.argtypes = [v, v, v, i64, v]
+    lib.otx_silu_backward.restype = i32
+    lib.otx_transpose_bf16.argtypes = [v, i32, i32, i32, v, i32, v]
+    lib.otx_transpose_bf16.restype = i32
+    lib.otx_colsum_bf16.argtypes = [v, i32, i32, i32, v, v]
+    lib.otx_colsum_bf16.restype = i32
+    lib.otx_adam.argtypes = [v, v, v, v, i32, i32, f32, f32, f32, f32, i32, v, i32, v, i32, v]
+    lib.otx_adam.restype = i32
     lib.otx_collect.argtypes = [P(Sensor), P(Rays), P(Image), v]
     lib.otx_collect.restype = i32
     lib.otx_sag_eval.argtypes = [P(System), i32, P(Rays), P(Rays), v]

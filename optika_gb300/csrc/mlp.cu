@@ -1,0 +1,496 @@
+// Tensor-core kernels of the learned surrogate (a BF16 MLP with FP32
+// accumulation) and its training step.
+//
+// k_gemm: C = epilogue(A B^T + bias) for row-major (K-major) BF16 A [M x K]
+// and B [N x K].  Tiles reach shared memory by TMA (cp.async.bulk.tensor,
+// 128-byte swizzle, zero fill outside the matrix) through a ring of
+// mbarrier-tracked stages; one elected thread issues tcgen05.mma (M = 128,
+// N = NT, K = 16 per instruction) into a TMEM accumulator; all four warps
+// read it back with tcgen05.ld for the epilogue.  Every mbarrier wait is
+// bounded: on timeout the kernel records an error flag, frees its TMEM and
+// returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <cmath>
+#include <mutex>
+
+#include "../../include/optika_gb300.h"
+
+namespace otx {
+
+constexpr int GEMM_STAGES = 4;
+constexpr int GEMM_BK = 64;  // bf16 elements per K chunk: 128 bytes
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the phase of the given parity: false after ~1 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int i = 0; i < (1 << 24); ++i) {
+    if (mbar_test(bar, parity)) return true;
+    if (i > 32) __nanosleep(64);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(slot)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// D[tmem] (+)= A[smem] B[smem]^T, kind::f16 (BF16 inputs, FP32 accumulate).
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Arrive on an mbarrier when every tcgen05.mma issued so far has completed.
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory matrix descriptor of a K-major tile with 128-byte swizzle:
+// rows of 128 bytes, 8-row groups 1024 bytes apart (SBO), descriptor
+// version 1, layout type SWIZZLE_128B.
+__device__ __forceinline__ uint64_t desc_sw128(const void* p) {
+  const uint64_t addr = smem_u32(p);
+  uint64_t d = (addr >> 4) & 0x3FFFull;
+  d |= 1ull << 16;             // leading byte offset (unused for swizzled K-major)
+  d |= (1024ull >> 4) << 32;   // stride byte offset: 8 rows x 128 B
+  d |= 1ull << 46;             // descriptor version
+  d |= 2ull << 61;             // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D FP32, A and B BF16, both K-major.
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ float silu(float z) { return z / (1.f + __expf(-z)); }
+
+struct GemmArgs {
+  int m;        // valid rows of A / C
+  int n;        // valid columns of C (rows of B)
+  int k;        // valid K
+  int ldo;      // elements between rows of the output
+  const float* bias;   // n entries or null
+  void* out;           // bf16 (EPI 0) or fp32 (EPI 1, 2)
+  __nv_bfloat16* z;    // pre-activation (EPI 0) or null
+  int* err;            // set to 1 on a timed-out wait
+};
+
+#define OTX_EPI_SILU_BF16 0
+#define OTX_EPI_BIAS_F32 1
+#define OTX_EPI_F32 2
+
+template <int NT, int EPI>
+__global__ void __launch_bounds__(128, 1)
+    k_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb,
+           const GemmArgs g) {
+  constexpr int A_BYTES = 128 * GEMM_BK * 2;  // 16 KB
+  constexpr int B_BYTES = NT * GEMM_BK * 2;
+  constexpr uint32_t NCOLS = NT < 32 ? 32 : NT;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint8_t* sa = smem;
+  uint8_t* sb = sa + GEMM_STAGES * A_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sb + GEMM_STAGES * B_BYTES);
+  uint64_t* empty = full + GEMM_STAGES;
+  uint64_t* done = empty + GEMM_STAGES;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(done + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * 128;
+  const int nk = (g.k + GEMM_BK - 1) / GEMM_BK;
+
+  if (tid == 0) {
+    for (int s = 0; s < GEMM_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tmem_alloc(tslot, NCOLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  int issued = 0;  // chunks whose TMA loads thread 0 started
+  if (tid == 0) {
+    // producer: stage s holds chunk k; reuse waits for the MMAs of chunk k - S
+    for (int k = 0; k < nk; ++k) {
+      const int s = k % GEMM_STAGES;
+      if (k >= GEMM_STAGES) {
+        if (!mbar_wait(&empty[s], ((k / GEMM_STAGES) - 1) & 1)) {
+          atomicExch(g.err, 1);
+          break;
+        }
+      }
+      mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
+      tma_load_2d(sa + s * A_BYTES, &ta, k * GEMM_BK, m0, &full[s]);
+      tma_load_2d(sb + s * B_BYTES, &tb, k * GEMM_BK, 0, &full[s]);
+      issued = k + 1;
+    }
+  } else if (tid == 32) {
+    // MMA issuer
+    constexpr uint32_t IDESC = idesc_bf16(128, NT);
+    bool ok = true;
+    for (int k = 0; k < nk; ++k) {
+      const int s = k % GEMM_STAGES;
+      if (!mbar_wait(&full[s], (k / GEMM_STAGES) & 1)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      const uint64_t ad = desc_sw128(sa + s * A_BYTES);
+      const uint64_t bd = desc_sw128(sb + s * B_BYTES);
+#pragma unroll
+      for (int kk = 0; kk < GEMM_BK / 16; ++kk)
+        umma_bf16(tbase, ad + 2 * kk, bd + 2 * kk, IDESC, (k | kk) != 0);
+      umma_commit(&empty[s]);
+    }
+    if (ok)
+      umma_commit(done);
+    else
+      atomicExch(g.err, 1);
+  }
+  __syncwarp();
+  const bool ok = mbar_wait(done, 0);
+  tc_fence_after();
+  if (!ok) {
+    if (lane == 0) atomicExch(g.err, 1);
+    // let the copies this CTA started land before its shared memory is
+    // released (bounded, as every wait here)
+    if (tid == 0) {
+      for (int k = issued - GEMM_STAGES > 0 ? issued - GEMM_STAGES : 0; k < issued; ++k)
+        mbar_wait(&full[k % GEMM_STAGES], (k / GEMM_STAGES) & 1);
+    }
+  } else {
+    // epilogue: warp w owns TMEM lanes (rows) 32 w .. 32 w + 31
+    const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c = 0; c < NT; c += 16) {
+      float v[16];
+      tmem_ld16(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+      if (row < g.m) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int col = c + i;
+          if (col < g.n) {
+            const float b = g.bias ? g.bias[col] : 0.f;
+            if (EPI == OTX_EPI_SILU_BF16) {
+              const float zz = v[i] + b;
+              reinterpret_cast<__nv_bfloat16*>(g.out)[(int64_t)row * g.ldo + col] =
+                  __float2bfloat16_rn(silu(zz));
+              if (g.z) g.z[(int64_t)row * g.ldo + col] = __float2bfloat16_rn(zz);
+            } else if (EPI == OTX_EPI_BIAS_F32) {
+              reinterpret_cast<float*>(g.out)[(int64_t)row * g.ldo + col] = v[i] + b;
+            } else {
+              reinterpret_cast<float*>(g.out)[(int64_t)row * g.ldo + col] = v[i];
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tbase, NCOLS);
+}
+
+// ---------------------------------------------------------------- elementwise
+
+// dZ = dY * silu'(Z), silu'(z) = s (1 + z (1 - s)), s = sigmoid(z); both bf16.
+__global__ void k_silu_backward(const float* __restrict__ dy, const __nv_bfloat16* __restrict__ z,
+                                __nv_bfloat16* __restrict__ dz, int64_t count) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float zz = __bfloat162float(z[i]);
+    const float s = 1.f / (1.f + __expf(-zz));
+    dz[i] = __float2bfloat16_rn(dy[i] * s * (1.f + zz * (1.f - s)));
+  }
+}
+
+// out[c][r] = in[r][c] for a rows x cols bf16 matrix (32 x 32 smem tiles).
+__global__ void k_transpose_bf16(const __nv_bfloat16* __restrict__ in, int rows, int cols, int ldi,
+                                 __nv_bfloat16* __restrict__ out, int ldo) {
+  __shared__ __nv_bfloat16 tile[32][33];
+  const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int r = by + j, c = bx + threadIdx.x;
+    if (r < rows && c < cols) tile[j][threadIdx.x] = in[(int64_t)r * ldi + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += blockDim.y) {
+    const int c = bx + j, r = by + threadIdx.x;
+    if (r < rows && c < cols) out[(int64_t)c * ldo + r] = tile[threadIdx.x][j];
+  }
+}
+
+// out[c] = sum_r in[r][c] (bf16 in, fp32 out), one block per column chunk.
+__global__ void k_colsum_bf16(const __nv_bfloat16* __restrict__ in, int rows, int cols, int ldi,
+                              float* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float acc = 0.f;
+  for (int r = blockIdx.y; r < rows; r += gridDim.y) acc += __bfloat162float(in[(int64_t)r * ldi + c]);
+  atomicAdd(out + c, acc);
+}
+
+// Adam (Kingma and Ba, 2015) on fp32 master weights; writes the bf16
+// weights and, if given, their transpose (rows x cols -> cols x rows).
+__global__ void k_adam(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
+                       const float* __restrict__ grad, int rows, int cols, float lr, float b1,
+                       float b2, float eps, float c1, float c2, __nv_bfloat16* __restrict__ w16,
+                       int ld16, __nv_bfloat16* __restrict__ w16t, int ld16t) {
+  const int64_t n = (int64_t)rows * cols;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float gi = grad[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    w[i] = wi;
+    const int r = (int)(i / cols), c = (int)(i % cols);
+    if (w16) w16[(int64_t)r * ld16 + c] = __float2bfloat16_rn(wi);
+    if (w16t) w16t[(int64_t)c * ld16t + r] = __float2bfloat16_rn(wi);
+  }
+}
+
+// ---------------------------------------------------------------- host
+
+typedef CUresult (*EncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiled encode_fn() {
+  static EncodeTiled fn = nullptr;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  }
+  return fn;
+}
+
+// 2-D bf16 tensor map: rows x cols (cols contiguous, row pitch ld elements),
+// box of box_rows x 64 with 128-byte swizzle; zero fill outside.
+static bool make_map(CUtensorMap* map, const void* base, int rows, int cols, int ld,
+                     int box_rows) {
+  EncodeTiled fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)GEMM_BK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int NT, int EPI>
+static otx_status launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g,
+                              cudaStream_t st) {
+  const size_t smem = 1024 + GEMM_STAGES * (128 * GEMM_BK * 2 + NT * GEMM_BK * 2) +
+                      (2 * GEMM_STAGES + 2) * 8;
+  static bool configured = false;
+  if (!configured) {
+    if (cudaFuncSetAttribute(k_gemm<NT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+      return OTX_ERR_CUDA;
+    configured = true;
+  }
+  const int grid = (g.m + 127) / 128;
+  k_gemm<NT, EPI><<<grid, 128, smem, st>>>(ta, tb, g);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+template <int EPI>
+static otx_status dispatch_nt(int nt, const CUtensorMap& ta, const CUtensorMap& tb,
+                              const GemmArgs& g, cudaStream_t st) {
+  switch (nt) {
+    case 16: return launch_gemm<16, EPI>(ta, tb, g, st);
+    case 64: return launch_gemm<64, EPI>(ta, tb, g, st);
+    case 128: return launch_gemm<128, EPI>(ta, tb, g, st);
+    case 256: return launch_gemm<256, EPI>(ta, tb, g, st);
+    default: return OTX_ERR_UNSUPPORTED;
+  }
+}
+
+static int grid_1d(int64_t n, int block) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 132;
+  const int64_t need = (n + block - 1) / block;
+  const int64_t cap = (int64_t)sms * 16;
+  return (int)(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
+}  // namespace otx
+
+using namespace otx;
+
+extern "C" {
+
+otx_status otx_gemm_bf16(const void* a, int32_t lda, const void* b, int32_t ldb, int32_t m,
+                         int32_t n, int32_t k, const float* bias, int32_t epilogue, void* out,
+                         int32_t ldo, void* z, int32_t* err, void* stream) {
+  if (!a || !b || !out || !err || m < 0 || n < 1 || k < 1) return OTX_ERR_INVALID;
+  if (m == 0) return OTX_OK;
+  if (lda < k || ldb < k || ldo < n || (lda * 2) % 16 || (ldb * 2) % 16) return OTX_ERR_INVALID;
+  if ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) return OTX_ERR_INVALID;
+  if (epilogue < OTX_EPI_SILU_BF16 || epilogue > OTX_EPI_F32) return OTX_ERR_INVALID;
+  int nt = 16;
+  while (nt < n) nt *= 2;
+  if (nt == 32) nt = 64;
+  if (nt > 256) return OTX_ERR_SIZE;
+  CUtensorMap ta, tb;
+  if (!make_map(&ta, a, m, k, lda, 128) || !make_map(&tb, b, n, k, ldb, nt)) return OTX_ERR_CUDA;
+  GemmArgs g{m, n, k, ldo, bias, out, reinterpret_cast<__nv_bfloat16*>(z), err};
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  switch (epilogue) {
+    case OTX_EPI_SILU_BF16: return dispatch_nt<OTX_EPI_SILU_BF16>(nt, ta, tb, g, st);
+    case OTX_EPI_BIAS_F32: return dispatch_nt<OTX_EPI_BIAS_F32>(nt, ta, tb, g, st);
+    default: return dispatch_nt<OTX_EPI_F32>(nt, ta, tb, g, st);
+  }
+}
+
+otx_status otx_silu_backward(const float* dy, const void* z, void* dz, int64_t count,
+                             void* stream) {
+  if (count < 0 || (count > 0 && (!dy || !z || !dz))) return OTX_ERR_INVALID;
+  if (count == 0) return OTX_OK;
+  k_silu_backward<<<grid_1d(count, 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      dy, reinterpret_cast<const __nv_bfloat16*>(z), reinterpret_cast<__nv_bfloat16*>(dz), count);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+otx_status otx_transpose_bf16(const void* in, int32_t rows, int32_t cols, int32_t ldi, void* out,
+                              int32_t ldo, void* stream) {
+  if (!in || !out || rows < 0 || cols < 0 || ldi < cols || ldo < rows) return OTX_ERR_INVALID;
+  if (rows == 0 || cols == 0) return OTX_OK;
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+  k_transpose_bf16<<<grid, block, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      reinterpret_cast<const __nv_bfloat16*>(in), rows, cols, ldi,
+      reinterpret_cast<__nv_bfloat16*>(out), ldo);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+otx_status otx_colsum_bf16(const void* in, int32_t rows, int32_t cols, int32_t ldi, float* out,
+                           void* stream) {
+  if (!in || !out || rows < 0 || cols < 0 || ldi < cols) return OTX_ERR_INVALID;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (cudaMemsetAsync(out, 0, sizeof(float) * (size_t)cols, st) != cudaSuccess) return OTX_ERR_CUDA;
+  if (rows == 0 || cols == 0) return OTX_OK;
+  dim3 grid((cols + 127) / 128, rows < 256 ? rows : 256);
+  k_colsum_bf16<<<grid, 128, 0, st>>>(reinterpret_cast<const __nv_bfloat16*>(in), rows, cols, ldi,
+                                      out);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+otx_status otx_adam(float* w, float* m, float* v, const float* grad, int32_t rows, int32_t cols,
+                    float lr, float beta1, float beta2, float eps, int32_t step, void* w16,
+                    int32_t ld16, void* w16t, int32_t ld16t, void* stream) {
+  if (!w || !m || !v || !grad || rows < 0 || cols < 0 || step < 1) return OTX_ERR_INVALID;
+  if ((w16 && ld16 < cols) || (w16t && ld16t < rows)) return OTX_ERR_INVALID;
+  const int64_t n = (int64_t)rows * cols;
+  if (n == 0) return OTX_OK;
+  float c1 = 1.f, c2 = 1.f;
+  {
+    const double p1 = std::pow((double)beta1, (double)step);
+    const double p2 = std::pow((double)beta2, (double)step);
+    c1 = (float)(1.0 / (1.0 - p1));
+    c2 = (float)(1.0 / (1.0 - p2));
+  }
+  k_adam<<<grid_1d(n, 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      w, m, v, grad, rows, cols, lr, beta1, beta2, eps, c1, c2,
+      reinterpret_cast<__nv_bfloat16*>(w16), ld16, reinterpret_cast<__nv_bfloat16*>(w16t), ld16t);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+}  // extern "C"
