@@ -179,7 +179,7 @@ def run_reference(args, rank: int, world: int) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--rays", type=int, default=100_000_000)
@@ -311,19 +311,28 @@ def main() -> None:
         "frac": achieved / pk["hbm_gbs"],
         "traffic": None,
         "peak_kind": pk_kind,
-        "kernel": "k_trace<rpt,GRID_INFINITY,false>",
+        "kernel": "k_trace_fixed<1, Object, Stop, ConicCoated, FlatCoated, Detector>",
         "kernel_ms": kernel_ms,
         "bytes_per_ray": BYTES_PER_RAY,
     }
+    # per-ray DRAM traffic and FP32 operation counts of this kernel, from one
+    # ncu capture of the same workload at 8e6 rays (scaled by the ray count)
     prof = ROOT / "profiles" / "trace_precision_1e8.json"
     if prof.exists():
         pj = json.loads(prof.read_text())
         if pj.get("dram_bytes_per_ray"):
             roofline["traffic"] = pj["dram_bytes_per_ray"] * n
         if pj.get("flops_per_ray"):
+            # the kernel is bound by FP32 instruction issue, not by HBM: its
+            # FP32 rate against the FP32 pipe's peak at the maximum SM clock
+            # (152 SMs x 128 lanes x 2 flops per FMA; nominal, not measured)
             fl = pj["flops_per_ray"]
-            roofline["fp32_flops_per_ray"] = fl
-            roofline["fp32_tflops_achieved"] = fl * n / (kernel_ms * 1e-3) / 1e12
+            fp32_peak = 152 * 128 * 2 * float(pk.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+            ach = fl * n / (kernel_ms * 1e-3) / 1e12
+            roofline["fp32"] = {"achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                                "frac": ach / fp32_peak, "flops_per_ray": fl,
+                                "peak_kind": "nominal at the measured maximum SM clock",
+                                "fma_pipe_active_pct_ncu": pj.get("fma_pipe_active_pct")}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
