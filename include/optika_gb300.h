@@ -254,6 +254,28 @@ typedef struct otx_batch {
   int32_t image_stride;             /* elements between config images     */
 } otx_batch;
 
+/* Learned surrogate of a batch's ray map: a BF16 MLP over 9 inputs (field
+ * x, y and pupil x, y normalised by their half ranges, wavelength by the
+ * half band about its centre, 4 normalised configuration parameters)
+ * predicting the image position as a residual (in out_scale mm units) over
+ * a per-configuration quadratic polynomial of the 5 ray inputs, plus a
+ * vignetting logit.  No counterpart in the reference. */
+#define OTX_SURROGATE_NIN 9    /* network inputs                            */
+#define OTX_SURROGATE_LDX 16   /* row pitch of the packed inputs (bf16)     */
+#define OTX_SURROGATE_NBASE 21 /* quadratic terms: 1, u_i, u_i u_j (i <= j) */
+
+typedef struct otx_surrogate {
+  int32_t num_configs;
+  int32_t pad_;
+  uint64_t config_inputs; /* device float[num_configs][4], normalised        */
+  uint64_t baseline;      /* device float[num_configs][2][NBASE]: x, y (mm)  */
+  uint64_t trusted;       /* device uint8[num_configs] or 0 (all trusted):   */
+                          /* rays of untrusted configurations are traced    */
+  float out_scale;        /* mm per unit of the position outputs            */
+  float logit_band;       /* rays with |logit| < logit_band are traced      */
+  float pad2_[2];
+} otx_surrogate;
+
 typedef struct otx_launch {
   int32_t rays_per_thread; /* 1, 2 or 4; 0 = library default          */
   int32_t block_size;      /* threads per CTA; 0 = library default     */
@@ -266,7 +288,7 @@ typedef struct otx_launch {
 /* ABI self-description: sizes of the descriptor structs, for binding
  * checks.  `which`: 0 otx_system, 1 otx_surface, 2 otx_rays, 3 otx_grid,
  * 4 otx_image, 5 otx_launch, 6 otx_affine, 7 otx_sensor, 8 otx_layer,
- * 9 otx_stack, 10 otx_periodic_stack, 11 otx_batch. */
+ * 9 otx_stack, 10 otx_periodic_stack, 11 otx_batch, 12 otx_surrogate. */
 int64_t otx_sizeof(int32_t which);
 int32_t otx_abi_version(void);
 const char* otx_status_string(otx_status s);
@@ -349,17 +371,23 @@ otx_status otx_multilayer_periodic(const otx_periodic_stack* configs, int32_t nu
 /* ---- learned surrogate (BF16 MLP on tensor cores) ------------------- */
 /* No counterpart in the reference: the surrogate of the ray map is new.   */
 
-#define OTX_EPI_SILU_BF16 0 /* out = bf16(silu(A B^T + bias)), z = bf16(pre) */
-#define OTX_EPI_BIAS_F32 1  /* out = f32(A B^T + bias)                       */
-#define OTX_EPI_F32 2       /* out = f32(A B^T)                              */
+#define OTX_EPI_SILU_BF16 0  /* out = bf16(silu(A B^T + bias)), z = bf16(pre)  */
+#define OTX_EPI_BIAS_F32 1   /* out = f32(A B^T + bias)                        */
+#define OTX_EPI_F32 2        /* out = f32(A B^T)                               */
+#define OTX_EPI_DSILU_BF16 3 /* out = bf16(A B^T * silu'(z)), z read           */
+#define OTX_EPI_F32_ATOMIC 4 /* out = f32(A B^T), K split over CTAs, summed    */
+                             /* by atomics into out (zeroed by the call)       */
 
 /* C[m x n] = epilogue(A B^T + bias): A bf16 [m x k] and B bf16 [n x k],
  * row-major with row pitches lda, ldb (elements, multiples of 8, rows
  * 16-byte aligned); tcgen05 tensor cores, TMA tiles, FP32 accumulation.
- * n <= 256.  *err (device int) is set if a bounded wait gave up. */
+ * n <= 256.  z has out's row pitch ldo.  out_t (bf16 epilogues only, may
+ * be null) receives the transpose of out with row pitch ldt >= m.  *err
+ * (device int) is set if a bounded wait gave up. */
 otx_status otx_gemm_bf16(const void* a, int32_t lda, const void* b, int32_t ldb, int32_t m,
                          int32_t n, int32_t k, const float* bias, int32_t epilogue, void* out,
-                         int32_t ldo, void* z, int32_t* err, void* stream);
+                         int32_t ldo, void* z, void* out_t, int32_t ldt, int32_t* err,
+                         void* stream);
 /* dz = dy * silu'(z) (dy fp32, z and dz bf16, count elements). */
 otx_status otx_silu_backward(const float* dy, const void* z, void* dz, int64_t count,
                              void* stream);
@@ -375,6 +403,35 @@ otx_status otx_colsum_bf16(const void* in, int32_t rows, int32_t cols, int32_t l
 otx_status otx_adam(float* w, float* m, float* v, const float* grad, int32_t rows, int32_t cols,
                     float lr, float beta1, float beta2, float eps, int32_t step, void* w16,
                     int32_t ld16, void* w16t, int32_t ld16t, void* stream);
+
+/* Network inputs of rays [first, first + count) of a batch (or of rays
+ * perm[first + r] when perm is given): x bf16 [count][OTX_SURROGATE_LDX]
+ * (columns 9.. zero), x_t (or null) its transpose with row pitch ldt, and
+ * aux float4 [count]: with training targets px, py, unvignetted (indexed
+ * by batch ray) {residual x, residual y (out_scale units), label, 0};
+ * without {baseline x, baseline y (mm), wavelength, configuration}. */
+otx_status otx_surrogate_pack(const otx_batch* batch, const otx_surrogate* sg, int64_t first,
+                              int64_t count, const int64_t* perm, const float* px,
+                              const float* py, const uint8_t* unvignetted, void* x, void* x_t,
+                              int32_t ldt, float* aux, void* stream);
+/* Training loss of network outputs y (fp32 [count][ldy]: residual x, y,
+ * logit) against aux targets: w_pos * sum(label * |dr|^2) + w_cls * sum(BCE),
+ * both times norm.  Writes dL/dy as bf16 [count][8] (columns 3.. zero) and
+ * its transpose dy_t [3][ldt]; adds {sum label |dr|^2, sum BCE, sum label,
+ * correct classifications} into sums[4]. */
+otx_status otx_surrogate_loss(const float* y, int32_t ldy, const float* aux, int64_t count,
+                              float w_pos, float w_cls, float norm, void* dy, void* dy_t,
+                              int32_t ldt, float* sums, void* stream);
+/* Image simulation of rays [first, first + count) of a batch from network
+ * outputs y and packed aux: rays of trusted configurations with |logit| >=
+ * logit_band land at baseline + out_scale * y (if logit > 0); the others
+ * are traced through base (with the batch's overrides) in the same kernel.
+ * Adds into the per-configuration images and stats[4] = {rays, traced,
+ * binned by the network, binned by the trace}. */
+otx_status otx_surrogate_image(const otx_system* base, const otx_batch* batch,
+                               const otx_surrogate* sg, int64_t first, int64_t count,
+                               const float* y, int32_t ldy, const float* aux,
+                               const otx_image* image, unsigned long long* stats, void* stream);
 
 /* Bin rays given in the sensor's local frame into count and flux images.
  * Replaces optika/sensors/_sensors.py:92-161 (ImagingSensor.collect, the

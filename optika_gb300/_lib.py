@@ -34,7 +34,7 @@ APER_FLAG_DIRECTION = 4
 APER_FLAG_TRANSFORM = 8
 RULE_NONE, RULE_CONSTANT, RULE_POLY1D, RULE_HOLOGRAPHIC = range(4)
 INPUT_RAYS, INPUT_GRID_INFINITY, INPUT_GRID_FINITE = range(3)
-EPI_SILU_BF16, EPI_BIAS_F32, EPI_F32 = range(3)
+EPI_SILU_BF16, EPI_BIAS_F32, EPI_F32, EPI_DSILU_BF16, EPI_F32_ATOMIC = range(5)
 SYS_FLAG_FINAL_IDENTITY = 1
 
 f32 = ctypes.c_float
@@ -230,6 +230,24 @@ class Batch(ctypes.Structure):
     ]
 
 
+SURROGATE_NIN = 9
+SURROGATE_LDX = 16
+SURROGATE_NBASE = 21
+
+
+class Surrogate(ctypes.Structure):
+    _fields_ = [
+        ("num_configs", i32),
+        ("pad_", i32),
+        ("config_inputs", u64),
+        ("baseline", u64),
+        ("trusted", u64),
+        ("out_scale", f32),
+        ("logit_band", f32),
+        ("pad2_", f32 * 2),
+    ]
+
+
 class Launch(ctypes.Structure):
     _fields_ = [
         ("rays_per_thread", i32),
@@ -252,6 +270,7 @@ LAYOUT = {
     9: Stack,
     10: PeriodicStack,
     11: Batch,
+    12: Surrogate,
 }
 
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "_lib" / "liboptika_gb300.so"
@@ -299,7 +318,7 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_trace_batch.restype = i32
     lib.otx_trace_batch_noalloc.argtypes = [P(System), P(Batch), P(Rays), P(Image), P(Launch), v]
     lib.otx_trace_batch_noalloc.restype = i32
-    lib.otx_gemm_bf16.argtypes = [v, i32, v, i32, i32, i32, i32, v, i32, v, i32, v, v, v]
+    lib.otx_gemm_bf16.argtypes = [v, i32, v, i32, i32, i32, i32, v, i32, v, i32, v, v, i32, v, v]
     lib.otx_gemm_bf16.restype = i32
     lib.otx_silu_backward.argtypes = [v, v, v, i64, v]
     lib.otx_silu_backward.restype = i32
@@ -309,6 +328,14 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_colsum_bf16.restype = i32
     lib.otx_adam.argtypes = [v, v, v, v, i32, i32, f32, f32, f32, f32, i32, v, i32, v, i32, v]
     lib.otx_adam.restype = i32
+    lib.otx_surrogate_pack.argtypes = [P(Batch), P(Surrogate), i64, i64, v, v, v, v, v, v, i32,
+                                       v, v]
+    lib.otx_surrogate_pack.restype = i32
+    lib.otx_surrogate_loss.argtypes = [v, i32, v, i64, f32, f32, f32, v, v, i32, v, v]
+    lib.otx_surrogate_loss.restype = i32
+    lib.otx_surrogate_image.argtypes = [P(System), P(Batch), P(Surrogate), i64, i64, v, i32, v,
+                                        P(Image), v, v]
+    lib.otx_surrogate_image.restype = i32
     lib.otx_collect.argtypes = [P(Sensor), P(Rays), P(Image), v]
     lib.otx_collect.restype = i32
     lib.otx_sag_eval.argtypes = [P(System), i32, P(Rays), P(Rays), v]

@@ -146,16 +146,58 @@ struct GemmArgs {
   int m;        // valid rows of A / C
   int n;        // valid columns of C (rows of B)
   int k;        // valid K
-  int ldo;      // elements between rows of the output
+  int ldo;      // elements between rows of the output (and of z)
+  int ldt;      // elements between rows of the transposed copy
+  int kc;       // K chunks per split (blockIdx.y selects the split)
+  int vec;      // rows of out / z start 16-byte aligned and n % 16 == 0
   const float* bias;   // n entries or null
-  void* out;           // bf16 (EPI 0) or fp32 (EPI 1, 2)
-  __nv_bfloat16* z;    // pre-activation (EPI 0) or null
+  void* out;           // bf16 (SILU, DSILU) or fp32 (BIAS_F32, F32, F32_ATOMIC)
+  __nv_bfloat16* z;    // SILU: pre-activation written; DSILU: pre-activation read
+  __nv_bfloat16* outT; // bf16 transposed copy of out (SILU, DSILU) or null
   int* err;            // set to 1 on a timed-out wait
 };
 
 #define OTX_EPI_SILU_BF16 0
 #define OTX_EPI_BIAS_F32 1
 #define OTX_EPI_F32 2
+#define OTX_EPI_DSILU_BF16 3
+#define OTX_EPI_F32_ATOMIC 4
+
+__device__ __forceinline__ void store16_bf16(__nv_bfloat16* p, const float v[16], int valid,
+                                             bool vec) {
+  if (vec && valid == 16) {
+    uint32_t w[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+      w[i] = *reinterpret_cast<uint32_t*>(&h);
+    }
+    reinterpret_cast<uint4*>(p)[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    reinterpret_cast<uint4*>(p)[1] = make_uint4(w[4], w[5], w[6], w[7]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+      if (i < valid) p[i] = __float2bfloat16_rn(v[i]);
+  }
+}
+
+__device__ __forceinline__ void load16_bf16(const __nv_bfloat16* p, float v[16], int valid,
+                                            bool vec) {
+  if (vec && valid == 16) {
+    const uint4 a = reinterpret_cast<const uint4*>(p)[0];
+    const uint4 b = reinterpret_cast<const uint4*>(p)[1];
+    const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const __nv_bfloat162 h = *reinterpret_cast<const __nv_bfloat162*>(&w[i]);
+      v[2 * i] = __low2float(h);
+      v[2 * i + 1] = __high2float(h);
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = i < valid ? __bfloat162float(p[i]) : 0.f;
+  }
+}
 
 template <int NT, int EPI>
 __global__ void __launch_bounds__(128, 1)
@@ -176,7 +218,11 @@ __global__ void __launch_bounds__(128, 1)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * 128;
-  const int nk = (g.k + GEMM_BK - 1) / GEMM_BK;
+  // this CTA's K chunks: [kb, kb + nk); the host makes every split non-empty
+  const int nk_all = (g.k + GEMM_BK - 1) / GEMM_BK;
+  const int kb = blockIdx.y * g.kc;
+  const int nk = min(nk_all, kb + g.kc) - kb;
+  if (nk <= 0) return;  // uniform over the CTA, before any barrier or TMEM use
 
   if (tid == 0) {
     for (int s = 0; s < GEMM_STAGES; ++s) {
@@ -204,8 +250,8 @@ __global__ void __launch_bounds__(128, 1)
         }
       }
       mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
-      tma_load_2d(sa + s * A_BYTES, &ta, k * GEMM_BK, m0, &full[s]);
-      tma_load_2d(sb + s * B_BYTES, &tb, k * GEMM_BK, 0, &full[s]);
+      tma_load_2d(sa + s * A_BYTES, &ta, (kb + k) * GEMM_BK, m0, &full[s]);
+      tma_load_2d(sb + s * B_BYTES, &tb, (kb + k) * GEMM_BK, 0, &full[s]);
       issued = k + 1;
     }
   } else if (tid == 32) {
@@ -245,28 +291,57 @@ __global__ void __launch_bounds__(128, 1)
   } else {
     // epilogue: warp w owns TMEM lanes (rows) 32 w .. 32 w + 31
     const int row = m0 + warp * 32 + lane;
+    const bool vec = g.vec != 0;
 #pragma unroll 1
     for (int c = 0; c < NT; c += 16) {
       float v[16];
+      __syncwarp();  // tcgen05.ld is warp-aligned: reconverge after the stores
       tmem_ld16(tbase + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-      if (row < g.m) {
+      const int valid = min(16, g.n - c);
+      if (row >= g.m || valid <= 0) continue;
+      const int64_t o = (int64_t)row * g.ldo + c;
+      if (EPI == OTX_EPI_F32_ATOMIC) {
+        float* p = reinterpret_cast<float*>(g.out) + o;
+        if (vec && valid == 16) {
+#pragma unroll
+          for (int i = 0; i < 16; i += 4)
+            atomicAdd(reinterpret_cast<float4*>(p + i), make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]));
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            if (i < valid) atomicAdd(p + i, v[i]);
+        }
+        continue;
+      }
+      if (EPI == OTX_EPI_F32 || EPI == OTX_EPI_BIAS_F32) {
+        float* p = reinterpret_cast<float*>(g.out) + o;
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          if (i < valid) p[i] = v[i] + (EPI == OTX_EPI_BIAS_F32 ? g.bias[c + i] : 0.f);
+        continue;
+      }
+      float r[16];
+      if (EPI == OTX_EPI_SILU_BF16) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-          const int col = c + i;
-          if (col < g.n) {
-            const float b = g.bias ? g.bias[col] : 0.f;
-            if (EPI == OTX_EPI_SILU_BF16) {
-              const float zz = v[i] + b;
-              reinterpret_cast<__nv_bfloat16*>(g.out)[(int64_t)row * g.ldo + col] =
-                  __float2bfloat16_rn(silu(zz));
-              if (g.z) g.z[(int64_t)row * g.ldo + col] = __float2bfloat16_rn(zz);
-            } else if (EPI == OTX_EPI_BIAS_F32) {
-              reinterpret_cast<float*>(g.out)[(int64_t)row * g.ldo + col] = v[i] + b;
-            } else {
-              reinterpret_cast<float*>(g.out)[(int64_t)row * g.ldo + col] = v[i];
-            }
-          }
+          v[i] += (g.bias && i < valid) ? g.bias[c + i] : 0.f;
+          r[i] = silu(v[i]);
         }
+        if (g.z) store16_bf16(g.z + o, v, valid, vec);
+      } else {  // DSILU: dZ = dH silu'(z), silu'(z) = s (1 + z (1 - s)), s = sigmoid(z)
+        float zz[16];
+        load16_bf16(g.z + o, zz, valid, vec);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const float sg = 1.f / (1.f + __expf(-zz[i]));
+          r[i] = v[i] * sg * (1.f + zz[i] * (1.f - sg));
+        }
+      }
+      store16_bf16(reinterpret_cast<__nv_bfloat16*>(g.out) + o, r, valid, vec);
+      if (g.outT) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          if (i < valid) g.outT[(int64_t)(c + i) * g.ldt + row] = __float2bfloat16_rn(r[i]);
       }
     }
   }
@@ -375,7 +450,7 @@ static bool make_map(CUtensorMap* map, const void* base, int rows, int cols, int
 
 template <int NT, int EPI>
 static otx_status launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g,
-                              cudaStream_t st) {
+                              int splits, cudaStream_t st) {
   const size_t smem = 1024 + GEMM_STAGES * (128 * GEMM_BK * 2 + NT * GEMM_BK * 2) +
                       (2 * GEMM_STAGES + 2) * 8;
   static bool configured = false;
@@ -385,19 +460,19 @@ static otx_status launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, cons
       return OTX_ERR_CUDA;
     configured = true;
   }
-  const int grid = (g.m + 127) / 128;
+  const dim3 grid((g.m + 127) / 128, splits);
   k_gemm<NT, EPI><<<grid, 128, smem, st>>>(ta, tb, g);
   return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
 }
 
 template <int EPI>
 static otx_status dispatch_nt(int nt, const CUtensorMap& ta, const CUtensorMap& tb,
-                              const GemmArgs& g, cudaStream_t st) {
+                              const GemmArgs& g, int splits, cudaStream_t st) {
   switch (nt) {
-    case 16: return launch_gemm<16, EPI>(ta, tb, g, st);
-    case 64: return launch_gemm<64, EPI>(ta, tb, g, st);
-    case 128: return launch_gemm<128, EPI>(ta, tb, g, st);
-    case 256: return launch_gemm<256, EPI>(ta, tb, g, st);
+    case 16: return launch_gemm<16, EPI>(ta, tb, g, splits, st);
+    case 64: return launch_gemm<64, EPI>(ta, tb, g, splits, st);
+    case 128: return launch_gemm<128, EPI>(ta, tb, g, splits, st);
+    case 256: return launch_gemm<256, EPI>(ta, tb, g, splits, st);
     default: return OTX_ERR_UNSUPPORTED;
   }
 }
@@ -420,24 +495,53 @@ extern "C" {
 
 otx_status otx_gemm_bf16(const void* a, int32_t lda, const void* b, int32_t ldb, int32_t m,
                          int32_t n, int32_t k, const float* bias, int32_t epilogue, void* out,
-                         int32_t ldo, void* z, int32_t* err, void* stream) {
+                         int32_t ldo, void* z, void* out_t, int32_t ldt, int32_t* err,
+                         void* stream) {
   if (!a || !b || !out || !err || m < 0 || n < 1 || k < 1) return OTX_ERR_INVALID;
-  if (m == 0) return OTX_OK;
+  if (epilogue < OTX_EPI_SILU_BF16 || epilogue > OTX_EPI_F32_ATOMIC) return OTX_ERR_INVALID;
   if (lda < k || ldb < k || ldo < n || (lda * 2) % 16 || (ldb * 2) % 16) return OTX_ERR_INVALID;
   if ((reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b)) & 15) return OTX_ERR_INVALID;
-  if (epilogue < OTX_EPI_SILU_BF16 || epilogue > OTX_EPI_F32) return OTX_ERR_INVALID;
+  if (epilogue == OTX_EPI_BIAS_F32 && !bias) return OTX_ERR_INVALID;
+  if (epilogue == OTX_EPI_DSILU_BF16 && !z) return OTX_ERR_INVALID;
+  const bool bf16_out = epilogue == OTX_EPI_SILU_BF16 || epilogue == OTX_EPI_DSILU_BF16;
+  if (out_t && (!bf16_out || ldt < m)) return OTX_ERR_INVALID;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (epilogue == OTX_EPI_F32_ATOMIC && m > 0 &&
+      cudaMemset2DAsync(out, (size_t)ldo * 4, 0, (size_t)n * 4, (size_t)m, st) != cudaSuccess)
+    return OTX_ERR_CUDA;
+  if (m == 0) return OTX_OK;
   int nt = 16;
   while (nt < n) nt *= 2;
   if (nt == 32) nt = 64;
   if (nt > 256) return OTX_ERR_SIZE;
   CUtensorMap ta, tb;
   if (!make_map(&ta, a, m, k, lda, 128) || !make_map(&tb, b, n, k, ldb, nt)) return OTX_ERR_CUDA;
-  GemmArgs g{m, n, k, ldo, bias, out, reinterpret_cast<__nv_bfloat16*>(z), err};
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const int esize = bf16_out ? 2 : 4;
+  const uintptr_t align = reinterpret_cast<uintptr_t>(out) |
+                          (epilogue == OTX_EPI_SILU_BF16 || epilogue == OTX_EPI_DSILU_BF16
+                               ? reinterpret_cast<uintptr_t>(z) : 0);
+  const int vec = (n % 16 == 0) && ((ldo * esize) % 16 == 0) && (align % 16 == 0);
+  const int nk_all = (k + GEMM_BK - 1) / GEMM_BK;
+  int kc = nk_all, splits = 1;
+  if (epilogue == OTX_EPI_F32_ATOMIC) {
+    // split K so that the grid fills the GPU: every split at least 2 chunks
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 132;
+    const int tiles = (m + 127) / 128;
+    const int want = max(1, (2 * sms) / tiles);
+    kc = max(2, (nk_all + want - 1) / want);
+    splits = (nk_all + kc - 1) / kc;
+  }
+  GemmArgs g{m, n, k, ldo, ldt, kc, vec, bias, out, reinterpret_cast<__nv_bfloat16*>(z),
+             reinterpret_cast<__nv_bfloat16*>(out_t), err};
   switch (epilogue) {
-    case OTX_EPI_SILU_BF16: return dispatch_nt<OTX_EPI_SILU_BF16>(nt, ta, tb, g, st);
-    case OTX_EPI_BIAS_F32: return dispatch_nt<OTX_EPI_BIAS_F32>(nt, ta, tb, g, st);
-    default: return dispatch_nt<OTX_EPI_F32>(nt, ta, tb, g, st);
+    case OTX_EPI_SILU_BF16: return dispatch_nt<OTX_EPI_SILU_BF16>(nt, ta, tb, g, splits, st);
+    case OTX_EPI_BIAS_F32: return dispatch_nt<OTX_EPI_BIAS_F32>(nt, ta, tb, g, splits, st);
+    case OTX_EPI_F32: return dispatch_nt<OTX_EPI_F32>(nt, ta, tb, g, splits, st);
+    case OTX_EPI_DSILU_BF16: return dispatch_nt<OTX_EPI_DSILU_BF16>(nt, ta, tb, g, splits, st);
+    default: return dispatch_nt<OTX_EPI_F32_ATOMIC>(nt, ta, tb, g, splits, st);
   }
 }
 

@@ -145,6 +145,7 @@ int64_t otx_sizeof(int32_t which) {
     case 9: return sizeof(otx_stack);
     case 10: return sizeof(otx_periodic_stack);
     case 11: return sizeof(otx_batch);
+    case 12: return sizeof(otx_surrogate);
     default: return -1;
   }
 }

@@ -13,24 +13,32 @@ from optika_gb300._api import ptr, stream_handle
 pytestmark = pytest.mark.gpu
 
 
-def _gemm(a, b, bias, epilogue, k=None):
+def _gemm(a, b, bias, epilogue, k=None, z_in=None, transposed=False):
     m = a.shape[0]
     k = a.shape[1] if k is None else k
     n = b.shape[0]
     lib = L.load()
     err = torch.zeros(1, dtype=torch.int32, device=a.device)
-    if epilogue == L.EPI_SILU_BF16:
+    out_t = None
+    if epilogue in (L.EPI_SILU_BF16, L.EPI_DSILU_BF16):
         out = torch.empty((m, n), dtype=torch.bfloat16, device=a.device)
-        z = torch.empty((m, n), dtype=torch.bfloat16, device=a.device)
+        z = z_in if z_in is not None else torch.empty((m, n), dtype=torch.bfloat16,
+                                                      device=a.device)
+        if transposed:
+            out_t = torch.full((n, m + 8), float("nan"), dtype=torch.bfloat16, device=a.device)
     else:
-        out = torch.empty((m, n), dtype=torch.float32, device=a.device)
+        out = torch.full((m, n), float("nan"), dtype=torch.float32, device=a.device)
         z = None
     st = lib.otx_gemm_bf16(ptr(a), a.stride(0), ptr(b), b.stride(0), m, n, k,
                            ptr(bias) if bias is not None else None, epilogue, ptr(out), n,
-                           ptr(z) if z is not None else None, ptr(err), stream_handle())
+                           ptr(z) if z is not None else None,
+                           ptr(out_t) if out_t is not None else None, m + 8, ptr(err),
+                           stream_handle())
     assert st == L.OK, lib.otx_status_string(st)
     torch.cuda.synchronize()
     assert err.item() == 0
+    if transposed:
+        return out, z, out_t
     return out, z
 
 
@@ -69,6 +77,41 @@ def test_gemm_matches_torch(cuda, m, n, k, epilogue):
         assert torch.allclose(z.float(), pre, atol=tol + 1e-2 * pre.abs().max().item(), rtol=1e-2)
         act = torch.nn.functional.silu(pre)
         assert torch.allclose(out.float(), act, atol=tol + 1e-2 * act.abs().max().item(), rtol=1e-2)
+
+
+@pytest.mark.parametrize("m,n,k", [(256, 256, 65536), (3, 256, 70000), (256, 9, 4096),
+                                   (200, 64, 128)])
+def test_gemm_split_k_atomic(cuda, m, n, k):
+    """Weight-gradient shape: small output, K = batch; K split across CTAs
+    and summed by float atomics."""
+    g = torch.Generator(device="cuda").manual_seed(k + m)
+    a = torch.randn((m, k), device="cuda", generator=g).to(torch.bfloat16)
+    b = torch.randn((n, k), device="cuda", generator=g).to(torch.bfloat16)
+    out, _ = _gemm(a, b, None, L.EPI_F32_ATOMIC)
+    ref = a.double() @ b.double().T
+    assert torch.allclose(out.double(), ref, atol=1e-3 * k ** 0.5, rtol=1e-4)
+
+
+@pytest.mark.parametrize("m,n,k", [(300, 256, 256), (1000, 256, 3), (129, 64, 64)])
+def test_gemm_dsilu_and_transposed_copy(cuda, m, n, k):
+    """Backward through SiLU: dZ = (dY W) * silu'(Z), with the transposed
+    copy the weight gradient consumes."""
+    g = torch.Generator(device="cuda").manual_seed(m + k)
+    k_store = (k + 7) // 8 * 8
+    a = _pad_k(torch.randn((m, k), device="cuda", generator=g).to(torch.bfloat16), k_store)
+    b = _pad_k(torch.randn((n, k), device="cuda", generator=g).to(torch.bfloat16), k_store)
+    z = (2 * torch.randn((m, n), device="cuda", generator=g)).to(torch.bfloat16)
+    out, _, out_t = _gemm(a, b, None, L.EPI_DSILU_BF16, k=k, z_in=z, transposed=True)
+    zf = z.float()
+    s = torch.sigmoid(zf)
+    ref = (a[:, :k].float() @ b[:, :k].float().T) * s * (1 + zf * (1 - s))
+    tol = 2e-3 * (k ** 0.5) + 1e-2 * ref.abs().max().item()
+    assert torch.allclose(out.float(), ref, atol=tol, rtol=1e-2)
+    assert torch.equal(out_t[:, :m], out.T)
+    # forward SiLU with the transposed copy of the activations
+    bias = torch.randn(n, device="cuda", generator=g)
+    h, zz, h_t = _gemm(a, b, bias, L.EPI_SILU_BF16, k=k, transposed=True)
+    assert torch.equal(h_t[:, :m], h.T)
 
 
 def test_elementwise_training_kernels(cuda):
