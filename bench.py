@@ -145,7 +145,7 @@ def run_reference(args, rank: int, world: int) -> None:
         return
     cores = len(os.sched_getaffinity(0))
     # each step: a bounded sample of the workload spread over all host cores
-    per_step = args.cpu_rays
+    per_step = args.ref_rays
     vals = []
     for i in range(args.warmup + args.steps):
         v, wall = cpu_baseline(per_step, cores)
@@ -176,6 +176,98 @@ def run_reference(args, rank: int, world: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_surrogate(args, rank: int, world: int) -> None:
+    """The learned form: a 9-256x4-3 BF16 MLP surrogate of the batched
+    spectrograph's ray map over 64 configurations, trained on 5e7 rays the
+    plain batched kernel traces, judged on 1e6 held-out rays, then used to
+    simulate the sensor images of 1e9 rays with plain-trace fallback.  The
+    same 1e9 rays through the plain batched kernel give the comparison.
+    Single GPU (replicas under torchrun)."""
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from optika_gb300 import configs
+    from optika_gb300.surrogate import RayMapSurrogate
+
+    n_cfg = 64
+    systems, _, params = configs.spectrograph_batch(n_cfg, seed=5)
+    sg = RayMapSurrogate(systems, params, wavelength=configs.SPEC_WAVELENGTH,
+                         field_half=configs.SPEC_FIELD_HALF, pupil_half=configs.SPEC_PUPIL_HALF,
+                         seed=5)
+    t0 = time.perf_counter()
+    train = sg.traced(np.full(n_cfg, 50_000_000 // n_cfg), seed=5 + 1000 * rank)
+    sg.fit_baseline(train)
+    torch.cuda.synchronize()
+    t_fit = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    hist = sg.train(train, steps=args.train_steps, batch=65536, lr=2e-3, log_every=500)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del train
+    torch.cuda.empty_cache()
+    held = sg.traced(np.full(n_cfg, 1_000_000 // n_cfg), seed=6 + 1000 * rank)
+    ev = sg.evaluate(held)
+    n_trusted = sg.set_trust(ev["per_config_rms_px"], 0.05)
+    ev_t = sg.evaluate(held)  # with untrusted configurations routed to the trace
+    del held
+
+    per_cfg = args.image_rays // n_cfg
+    img = sg.traced(np.full(n_cfg, per_cfg), seed=7 + 1000 * rank, image=True, outputs=())
+    total = img.total
+    for _ in range(max(1, args.warmup)):
+        sg.image(img, chunk=131072)
+        img.run()
+    torch.cuda.synchronize()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    e0.record()
+    _, stats = sg.image(img, chunk=131072)
+    e1.record()
+    sim = img.images.clone()
+    e2.record()
+    torch.cuda.synchronize()
+    ms_sur = e0.elapsed_time(e1)
+    st = stats.cpu().numpy()
+    p0, p1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+    p0.record()
+    img.run()
+    p1.record()
+    torch.cuda.synchronize()
+    ms_plain = p0.elapsed_time(p1)
+    ref = img.images
+    flux_err = abs(float(sim.sum()) - float(ref.sum())) / float(ref.sum())
+    l1 = float((sim.double() - ref.double()).abs().sum()) / float(ref.sum())
+    surfaces = 4
+    line = {
+        "metric": "rays*surfaces/s (image simulation: MLP surrogate + traced fallback vs plain "
+                  "FP32 trace)",
+        "value": total * surfaces / (ms_sur * 1e-3),
+        "unit": "rays*surfaces/s",
+        "n_gpus": world,
+        "higher_is_better": True,
+        "dtype": "bf16 (network), f32 (trace)",
+        "data": "synthetic (seeded Philox rays on the device)",
+        "config": {"workload": "spectrograph-surrogate", "configs": n_cfg,
+                   "train_rays": 50_000_000, "held_out_rays": 1_000_000, "image_rays": total,
+                   "network": "9-256-256-256-256-3 SiLU, BF16 weights, FP32 accumulation"},
+        "plain_trace": {"value": total * surfaces / (ms_plain * 1e-3), "ms": ms_plain},
+        "surrogate_ms": ms_sur,
+        "speedup_vs_plain": ms_plain / ms_sur,
+        "held_out": {k: ev[k] for k in ("rms_px", "p999_px", "max_px", "baseline_rms_px",
+                                        "baseline_p999_px", "fallback_fraction",
+                                        "efficiency_rel_error", "false_pass", "false_block")},
+        "held_out_after_trust": {k: ev_t[k] for k in ("rms_px", "p999_px", "fallback_fraction",
+                                                      "efficiency_rel_error")},
+        "trusted_configs": n_trusted,
+        "image": {"rays": int(st[0]), "traced": int(st[1]), "binned_by_network": int(st[2]),
+                  "binned_by_trace": int(st[3]), "flux_rel_error_vs_plain": flux_err,
+                  "l1_rel_diff_vs_plain": l1},
+        "training": {"steps": args.train_steps, "batch": 65536, "seconds": t_train,
+                     "fit_seconds": t_fit, "last": hist[-1]},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -185,7 +277,12 @@ def main() -> None:
     ap.add_argument("--rays", type=int, default=100_000_000)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-rays", type=int, default=8_000_000)
+    ap.add_argument("--ref-rays", type=int, default=2_000_000,
+                    help="rays per step of the reference (CPU) arm")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="precision", choices=["precision", "surrogate"])
+    ap.add_argument("--train-steps", type=int, default=6000)
+    ap.add_argument("--image-rays", type=int, default=1_000_000_000)
     ap.add_argument("--rays-per-thread", type=int, default=0)
     args = ap.parse_args()
 
@@ -195,6 +292,9 @@ def main() -> None:
 
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "surrogate":
+        run_surrogate(args, rank, world)
         return
 
     import torch

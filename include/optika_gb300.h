@@ -409,11 +409,13 @@ otx_status otx_adam(float* w, float* m, float* v, const float* grad, int32_t row
  * (columns 9.. zero), x_t (or null) its transpose with row pitch ldt, and
  * aux float4 [count]: with training targets px, py, unvignetted (indexed
  * by batch ray) {residual x, residual y (out_scale units), label, 0};
- * without {baseline x, baseline y (mm), wavelength, configuration}. */
+ * without {baseline x, baseline y (mm), wavelength, configuration}.
+ * u (or null) float [count][8] receives the FP32 normalised ray inputs
+ * u0..u4 and the configuration, for fitting the baseline. */
 otx_status otx_surrogate_pack(const otx_batch* batch, const otx_surrogate* sg, int64_t first,
                               int64_t count, const int64_t* perm, const float* px,
                               const float* py, const uint8_t* unvignetted, void* x, void* x_t,
-                              int32_t ldt, float* aux, void* stream);
+                              int32_t ldt, float* aux, float* u, void* stream);
 /* Training loss of network outputs y (fp32 [count][ldy]: residual x, y,
  * logit) against aux targets: w_pos * sum(label * |dr|^2) + w_cls * sum(BCE),
  * both times norm.  Writes dL/dy as bf16 [count][8] (columns 3.. zero) and

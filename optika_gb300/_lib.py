@@ -329,7 +329,7 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_adam.argtypes = [v, v, v, v, i32, i32, f32, f32, f32, f32, i32, v, i32, v, i32, v]
     lib.otx_adam.restype = i32
     lib.otx_surrogate_pack.argtypes = [P(Batch), P(Surrogate), i64, i64, v, v, v, v, v, v, i32,
-                                       v, v]
+                                       v, v, v]
     lib.otx_surrogate_pack.restype = i32
     lib.otx_surrogate_loss.argtypes = [v, i32, v, i64, f32, f32, f32, v, v, i32, v, v]
     lib.otx_surrogate_loss.restype = i32

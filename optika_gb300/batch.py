@@ -53,8 +53,11 @@ class BatchedTrace:
         if not base.object_is_at_infinity:
             raise NotImplementedError("batched traces generate objects at infinity")
         surfaces0 = base.surfaces_all
-        final = rigid_inverse(matrix_of(base.sensor.transformation)) @ matrix_of(
-            surfaces0[-1].transformation)
+        if surfaces0[-1] is base.sensor:
+            final = np.eye(4)  # exactly: the last surface is the sensor
+        else:
+            final = rigid_inverse(matrix_of(base.sensor.transformation)) @ matrix_of(
+                surfaces0[-1].transformation)
         pre = rigid_inverse(matrix_of(base.transformation)) @ matrix_of(base.object.transformation)
         self.lowering = lower_surfaces(surfaces0, pre=pre, final=final,
                                        input_mode=L.INPUT_GRID_INFINITY,

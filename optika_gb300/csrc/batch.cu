@@ -115,6 +115,8 @@ extern "C" otx_status otx_trace_batch(const otx_system* base, const otx_batch* b
   if (base->abi_version != OTX_ABI_VERSION) return OTX_ERR_INVALID;
   if (base->num_surfaces < 1 || base->num_surfaces > OTX_MAX_SURFACES) return OTX_ERR_SIZE;
   if (base->input_mode != OTX_INPUT_GRID_INFINITY) return OTX_ERR_INVALID;
+  // rays are stored in the last surface's frame: it must be the output frame
+  if (!(base->flags & OTX_SYS_FLAG_FINAL_IDENTITY)) return OTX_ERR_UNSUPPORTED;
   const otx_batch& b = *batch;
   if (b.num_configs < 0 || b.num_tiles < 0 || b.tile_size < 1) return OTX_ERR_INVALID;
   if (b.num_overrides < 0 || b.num_overrides > OTX_BATCH_MAX_OVERRIDES) return OTX_ERR_SIZE;
@@ -250,6 +252,8 @@ extern "C" otx_status otx_trace_batch_noalloc(const otx_system* base, const otx_
   if (base->abi_version != OTX_ABI_VERSION) return OTX_ERR_INVALID;
   if (base->num_surfaces < 1 || base->num_surfaces > OTX_MAX_SURFACES) return OTX_ERR_SIZE;
   if (base->input_mode != OTX_INPUT_GRID_INFINITY) return OTX_ERR_INVALID;
+  // rays are stored in the last surface's frame: it must be the output frame
+  if (!(base->flags & OTX_SYS_FLAG_FINAL_IDENTITY)) return OTX_ERR_UNSUPPORTED;
   const otx_batch& b = *batch;
   if (b.num_configs < 0 || b.num_tiles < 0 || b.tile_size < 1) return OTX_ERR_INVALID;
   if (b.num_tiles > OTX_NOALLOC_MAX_TILES) return OTX_ERR_SIZE;

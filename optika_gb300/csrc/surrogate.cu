@@ -79,6 +79,7 @@ struct PackArgs {
   __nv_bfloat16* xt;
   int ldt;
   float4* aux;
+  float4* u;  // 2 per row: u0..u3, then u4, config, 0, 0 (or null)
 };
 
 __global__ void __launch_bounds__(256) k_surrogate_pack(const __grid_constant__ PackArgs a) {
@@ -111,6 +112,10 @@ __global__ void __launch_bounds__(256) k_surrogate_pack(const __grid_constant__ 
 #pragma unroll
       for (int j = 0; j < OTX_SURROGATE_NIN; ++j)
         a.xt[(int64_t)j * a.ldt + r] = __float2bfloat16_rn(f[j]);
+    }
+    if (a.u) {
+      a.u[2 * r] = make_float4(f[0], f[1], f[2], f[3]);
+      a.u[2 * r + 1] = make_float4(f[4], (float)cfg, 0.f, 0.f);
     }
     float bx, by;
     baseline_xy(coef + (int64_t)cfg * 2 * OTX_SURROGATE_NBASE, f, bx, by);
@@ -240,16 +245,17 @@ __global__ void __launch_bounds__(SG_IMAGE_BLOCK)
     }
   }
   atomicAdd(&s_net, net);
-  // copy the base surfaces once; each configuration's overrides go on top
-  {
+  __syncthreads();
+  const int nfb = s_nfb;
+  int traced_binned = 0;
+  if (nfb > 0) {
+    // the base surfaces once; each configuration's overrides go on top
     const int words = sys.num_surfaces * (int)(sizeof(otx_surface) / 4);
     const int* src = reinterpret_cast<const int*>(sys.surfaces);
     int* dst = reinterpret_cast<int*>(surf);
     for (int w = tid; w < words; w += SG_IMAGE_BLOCK) dst[w] = src[w];
+    __syncthreads();  // nfb is uniform: every thread reaches this barrier
   }
-  __syncthreads();
-  const int nfb = s_nfb;
-  int traced_binned = 0;
   if (nfb > 0) {
     const int c_lo = min(max((int)a.aux[r0].w, 0), a.b.num_configs - 1);
     const int c_hi = min(max((int)a.aux[r1 - 1].w, 0), a.b.num_configs - 1);
@@ -314,8 +320,9 @@ extern "C" {
 otx_status otx_surrogate_pack(const otx_batch* batch, const otx_surrogate* sg, int64_t first,
                               int64_t count, const int64_t* perm, const float* px,
                               const float* py, const uint8_t* unvignetted, void* x, void* x_t,
-                              int32_t ldt, float* aux, void* stream) {
+                              int32_t ldt, float* aux, float* u, void* stream) {
   if (!batch_ok(batch, sg) || first < 0 || count < 0 || !x || !aux) return OTX_ERR_INVALID;
+  if (reinterpret_cast<uintptr_t>(u) & 15) return OTX_ERR_INVALID;
   if ((px || py || unvignetted) && !(px && py && unvignetted)) return OTX_ERR_INVALID;
   if (x_t && ldt < count) return OTX_ERR_INVALID;
   if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(aux)) & 15)
@@ -335,6 +342,7 @@ otx_status otx_surrogate_pack(const otx_batch* batch, const otx_surrogate* sg, i
   a.xt = reinterpret_cast<__nv_bfloat16*>(x_t);
   a.ldt = ldt;
   a.aux = reinterpret_cast<float4*>(aux);
+  a.u = reinterpret_cast<float4*>(u);
   k_surrogate_pack<<<grid_for(count, 256), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(a);
   return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
 }
