@@ -310,6 +310,32 @@ otx_status otx_trace_grid(const otx_system* sys, const otx_grid* in,
                           const otx_rays* out, const otx_image* image,
                           const otx_launch* launch, void* stream);
 
+/* otx_trace_grid for grid inputs and ray outputs in HOST memory (page-locked
+ * for full speed; pageable works but its copies do not overlap).
+ * Replaces the same call chain as otx_trace_grid, for callers whose arrays
+ * live on the host as the reference's NumPy arrays do
+ * (optika/systems/_sequential.py:791-988 take and return host arrays).
+ * The rays pass through the GPU in chunks: the host->device copy of one
+ * chunk, the trace of the previous one and the device->host copy of the one
+ * before that overlap on two library-owned copy streams and `stream`.
+ * Host input strides must be 0 (scalar) or 1.  `out` holds host pointers
+ * (accumulate: surface_stride >= count, as in otx_trace_grid); `image`
+ * holds DEVICE pointers, accumulated over every chunk.  `workspace` is
+ * caller-owned device memory, 256-byte aligned, of workspace_bytes; a
+ * smaller workspace than otx_trace_grid_host_workspace() recommends gives
+ * smaller chunks (OTX_ERR_SIZE if not even one ray fits).  Stream-ordered:
+ * the host outputs are complete when `stream` reaches the point after the
+ * call.  The first call on a device creates its copy streams and events. */
+otx_status otx_trace_grid_host(const otx_system* sys, const otx_grid* in_host,
+                               const otx_rays* out_host, const otx_image* image,
+                               const otx_launch* launch, void* workspace,
+                               int64_t workspace_bytes, void* stream);
+/* Recommended workspace bytes of otx_trace_grid_host for these inputs and
+ * outputs (`surfaces` output planes: the system's surface count when
+ * accumulating, else 1); -1 for invalid arguments. */
+int64_t otx_trace_grid_host_workspace(const otx_grid* in_host, const otx_rays* out_host,
+                                      int32_t surfaces);
+
 /* Multilayer reflectivity / transmissivity of `count` samples (float-float
  * transfer matrices).
  * Replaces optika/materials/_multilayers.py:240-532 (multilayer_efficiency).

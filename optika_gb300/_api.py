@@ -229,11 +229,119 @@ def _to_ray_array_partial(b: dict, shape: tuple) -> RayVectorArray:
     )
 
 
+def _is_host(values) -> bool:
+    """True when every tensor argument is a CPU torch tensor (and at least one is)."""
+    ts = [v for v in values if isinstance(v, torch.Tensor)]
+    return bool(ts) and all(t.device.type == "cpu" for t in ts)
+
+
+def _host_field(x, n: int, shape: tuple) -> tuple[torch.Tensor, int]:
+    t = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x, dtype=np.float32))
+    t = t.to(torch.float32)
+    if t.numel() == 1:
+        return t.reshape(1).contiguous(), 0
+    t = t.expand(shape).reshape(-1)
+    return t.contiguous(), 1
+
+
+def trace_grid_host(system, *, wavelength, field, pupil, intensity=None, accumulate: bool,
+                    final_local: bool, image: bool = False, wavelength_bins=None,
+                    launch: L.Launch | None = None, outputs=OUTPUT_FIELDS) -> RayFunctionArray:
+    """:func:`trace_grid` for host (CPU tensor) inputs, with host outputs.
+
+    The rays stream through the GPU in chunks (``otx_trace_grid_host``):
+    copies in, traces and copies out overlap.  Outputs are page-locked CPU
+    tensors, complete on return (the call synchronises the current stream),
+    as the reference's NumPy results are; images are copied to the host
+    too.  Page-locked inputs (``tensor.pin_memory()``) give full speed."""
+    dev = device()
+    surfaces = system.surfaces_all
+    obj = system.object
+    pre = rigid_inverse(matrix_of(system.transformation)) @ (
+        matrix_of(obj.transformation) if obj is not None else np.eye(4)
+    )
+    sensor = system.sensor
+    final = None
+    if final_local:
+        if sensor is None:
+            raise ValueError("rayfunction needs a sensor")
+        final = rigid_inverse(matrix_of(sensor.transformation)) @ matrix_of(
+            surfaces[-1].transformation)
+    mode = L.INPUT_GRID_INFINITY if system.object_is_at_infinity else L.INPUT_GRID_FINITE
+    lw = lower_surfaces(surfaces, pre=pre, final=final, input_mode=mode,
+                        sensor=sensor if image else None, wavelength_bins=wavelength_bins,
+                        device=dev)
+    vals = [wavelength, field.x, field.y, pupil.x, pupil.y]
+    if intensity is not None:
+        vals.append(intensity)
+    shapes = [tuple(v.shape) if isinstance(v, torch.Tensor) else np.shape(v) for v in vals]
+    shape = tuple(torch.broadcast_shapes(*shapes))
+    n = int(np.prod(shape)) if len(shape) else 1
+    fs = [_host_field(v, n, shape) for v in vals]
+    # field x/y share a stride, as do pupil x/y: expand the scalar of a mixed pair
+    for a, b in ((1, 2), (3, 4)):
+        if fs[a][1] != fs[b][1]:
+            fs[a] = (fs[a][0].expand(n).contiguous(), 1) if fs[a][1] == 0 else fs[a]
+            fs[b] = (fs[b][0].expand(n).contiguous(), 1) if fs[b][1] == 0 else fs[b]
+    g = L.Grid()
+    g.wavelength, g.field_x, g.field_y, g.pupil_x, g.pupil_y = (ptr(f[0]) for f in fs[:5])
+    g.stride_wavelength, g.stride_field, g.stride_pupil = fs[0][1], fs[1][1], fs[3][1]
+    if intensity is not None:
+        g.intensity, g.stride_intensity = ptr(fs[5][0]), fs[5][1]
+    g.count = n
+    S = len(surfaces)
+    full = (S, n) if accumulate else (n,)
+    bufs = {}
+    for k in OUTPUT_FIELDS:
+        if k not in outputs:
+            bufs[k] = None
+            continue
+        dt = torch.uint8 if k == "unvignetted" else (torch.float64 if k == "opl" else torch.float32)
+        bufs[k] = torch.empty(full, dtype=dt, pin_memory=True)
+    out = _rays_struct(bufs, n, n if accumulate else 0)
+    counts = flux = None
+    img = L.Image()
+    if image:
+        counts, flux, img = _image_buffers(sensor, wavelength_bins, dev)
+    ln = launch if launch is not None else L.Launch()
+    ln.accumulate = 1 if accumulate else 0
+    lib = L.load()
+    need = int(lib.otx_trace_grid_host_workspace(ctypes.byref(g), ctypes.byref(out),
+                                                 S if accumulate else 1))
+    if need < 0:
+        raise ValueError("invalid host trace arguments")
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    st = lib.otx_trace_grid_host(ctypes.byref(lw.sys), ctypes.byref(g), ctypes.byref(out),
+                                 ctypes.byref(img), ctypes.byref(ln), ptr(ws), need,
+                                 stream_handle())
+    L.check(st, "otx_trace_grid_host")
+    host_img = None
+    if image:
+        host_img = (torch.empty(counts.shape, dtype=counts.dtype, pin_memory=True),
+                    torch.empty(flux.shape, dtype=flux.dtype, pin_memory=True))
+        host_img[0].copy_(counts, non_blocking=True)
+        host_img[1].copy_(flux, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    del ws
+    rays = _to_ray_array_partial(bufs, shape)
+    return RayFunctionArray(inputs=None, outputs=rays, image=host_img)
+
+
 def trace_grid(system, *, wavelength, field, pupil, intensity=None, accumulate: bool,
                final_local: bool, image: bool = False, wavelength_bins=None,
                launch: L.Launch | None = None, outputs=OUTPUT_FIELDS) -> RayFunctionArray:
     """Input rays from (wavelength, field, pupil), traced through
-    ``system.surfaces_all`` (optika/systems/_sequential.py:791-988)."""
+    ``system.surfaces_all`` (optika/systems/_sequential.py:791-988).
+
+    CPU tensor inputs take the streamed host path (:func:`trace_grid_host`)
+    and give CPU outputs; anything else is moved to the GPU and gives GPU
+    tensors."""
+    vals = [wavelength, field.x, field.y, pupil.x, pupil.y, intensity]
+    if _is_host(vals):
+        return trace_grid_host(system, wavelength=wavelength, field=field, pupil=pupil,
+                               intensity=intensity, accumulate=accumulate,
+                               final_local=final_local, image=image,
+                               wavelength_bins=wavelength_bins, launch=launch, outputs=outputs)
     p = PreparedTrace(system, wavelength=wavelength, field=field, pupil=pupil,
                       intensity=intensity, accumulate=accumulate, final_local=final_local,
                       image=image, wavelength_bins=wavelength_bins, launch=launch,

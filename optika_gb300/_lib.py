@@ -306,6 +306,11 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_trace_rays.restype = i32
     lib.otx_trace_grid.argtypes = [P(System), P(Grid), P(Rays), P(Image), P(Launch), v]
     lib.otx_trace_grid.restype = i32
+    lib.otx_trace_grid_host.argtypes = [P(System), P(Grid), P(Rays), P(Image), P(Launch), v, i64,
+                                        v]
+    lib.otx_trace_grid_host.restype = i32
+    lib.otx_trace_grid_host_workspace.argtypes = [P(Grid), P(Rays), i32]
+    lib.otx_trace_grid_host_workspace.restype = i64
     lib.otx_multilayer_efficiency.argtypes = [
         P(System), i64, v, i64, v, i64, v, v, i64, v, v, v, v, v, v,
     ]

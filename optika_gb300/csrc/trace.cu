@@ -4,6 +4,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <mutex>
+
 #include "../../include/optika_gb300.h"
 #include "trace_kernel_decl.h"
 
@@ -125,11 +127,322 @@ static otx_status launch_trace(const otx_system* sys_in, int mode, const TraceAr
   return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------- host staging
+
+// Two ways for host arrays.  Page-locked arrays that the GPU addresses at
+// their host address (every pinned allocation under unified addressing,
+// as on GB300 where the GPU reaches Grace memory over NVLink-C2C) are read
+// and written by the trace kernel itself: one launch, no staging, the
+// loads and stores crossing C2C at the link's rate.  Other (pageable)
+// arrays are staged through the GPU in chunks: slot s of the workspace
+// holds one chunk's strided inputs and its outputs; chunk i's
+// host->device copy runs on the copy-in stream, its trace on the caller's
+// stream and its device->host copy on the copy-out stream, so with three
+// slots the copy in of chunk i + 1, the trace of chunk i and the copy out
+// of chunk i - 1 overlap.
+constexpr int HOST_SLOTS = 3;
+constexpr int HOST_MAX_DEVICES = 64;
+constexpr int64_t HOST_ALIGN = 256;
+constexpr int64_t HOST_HEAD = 256;  // broadcast scalars of the grid
+constexpr int HOST_TARGET_CHUNKS = 16;
+constexpr int64_t HOST_MIN_CHUNK = 1 << 20;
+
+struct HostPipe {
+  bool ready = false;
+  cudaStream_t in = nullptr, out = nullptr;
+  cudaEvent_t start = nullptr, end = nullptr;
+  cudaEvent_t copied[HOST_SLOTS], traced[HOST_SLOTS], drained[HOST_SLOTS];
+};
+
+static HostPipe g_pipes[HOST_MAX_DEVICES];
+static std::mutex g_pipe_mu;
+
+static otx_status host_pipe(HostPipe** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= HOST_MAX_DEVICES)
+    return OTX_ERR_CUDA;
+  HostPipe& p = g_pipes[dev];
+  if (!p.ready) {
+    const unsigned f = cudaEventDisableTiming;
+    if (cudaStreamCreateWithFlags(&p.in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&p.out, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p.start, f) != cudaSuccess ||
+        cudaEventCreateWithFlags(&p.end, f) != cudaSuccess)
+      return OTX_ERR_CUDA;
+    for (int s = 0; s < HOST_SLOTS; ++s) {
+      if (cudaEventCreateWithFlags(&p.copied[s], f) != cudaSuccess ||
+          cudaEventCreateWithFlags(&p.traced[s], f) != cudaSuccess ||
+          cudaEventCreateWithFlags(&p.drained[s], f) != cudaSuccess)
+        return OTX_ERR_CUDA;
+    }
+    p.ready = true;
+  }
+  *out = &p;
+  return OTX_OK;
+}
+
+static int64_t align_up(int64_t x) { return (x + HOST_ALIGN - 1) / HOST_ALIGN * HOST_ALIGN; }
+
+// The output fields of otx_rays in declaration order with their element sizes.
+static void out_fields(const otx_rays* r, uint64_t* ptrs[12], int sizes[12]) {
+  otx_rays* m = const_cast<otx_rays*>(r);
+  uint64_t* p[12] = {&m->px, &m->py, &m->pz, &m->dx, &m->dy, &m->dz, &m->wavelength,
+                     &m->intensity, &m->attenuation, &m->index_refraction, &m->unvignetted,
+                     &m->opl};
+  for (int i = 0; i < 12; ++i) {
+    ptrs[i] = p[i];
+    sizes[i] = i == 10 ? 1 : (i == 11 ? 8 : 4);
+  }
+}
+
+struct HostPlan {
+  int64_t chunk = 0;     // rays per chunk
+  int64_t slot = 0;      // bytes per slot
+  int64_t needed = 0;    // workspace bytes for this plan
+  int surfaces = 1;      // output planes (accumulate: one per surface)
+};
+
+// Inputs: the five grid arrays and the intensity, each strided (stride 1,
+// staged per chunk) or broadcast (stride 0, staged once in the head).
+static void grid_fields(const otx_grid* g, uint64_t ptrs[6], int64_t strides[6]) {
+  const uint64_t p[6] = {g->wavelength, g->field_x, g->field_y, g->pupil_x, g->pupil_y,
+                         g->intensity};
+  const int64_t s[6] = {g->stride_wavelength, g->stride_field, g->stride_field,
+                        g->stride_pupil, g->stride_pupil, g->stride_intensity};
+  for (int i = 0; i < 6; ++i) {
+    ptrs[i] = p[i];
+    strides[i] = s[i];
+  }
+}
+
+static int64_t slot_bytes(const otx_grid* g, const otx_rays* o, int surfaces, int64_t chunk) {
+  uint64_t gp[6];
+  int64_t gs[6];
+  grid_fields(g, gp, gs);
+  int64_t b = 0;
+  for (int i = 0; i < 6; ++i)
+    if (gp[i] && gs[i] != 0) b += align_up(chunk * 4);
+  uint64_t* op[12];
+  int sz[12];
+  out_fields(o, op, sz);
+  for (int i = 0; i < 12; ++i)
+    if (*op[i]) b += align_up(chunk * sz[i] * (int64_t)surfaces);
+  return b;
+}
+
+// True when the GPU addresses [p, p + bytes) at p: page-locked host memory
+// mapped at the same address (checked at both ends of the range).
+static bool mapped_same(uint64_t p, int64_t bytes) {
+  if (!p || bytes <= 0) return true;
+  const uint64_t ends[2] = {p, p + (uint64_t)bytes - 1};
+  for (uint64_t q : ends) {
+    cudaPointerAttributes at;
+    memset(&at, 0, sizeof(at));
+    if (cudaPointerGetAttributes(&at, reinterpret_cast<void*>(q)) != cudaSuccess) {
+      cudaGetLastError();  // clear the sticky-free error of an unknown pointer
+      return false;
+    }
+    if (at.type != cudaMemoryTypeHost || reinterpret_cast<uint64_t>(at.devicePointer) != q)
+      return false;
+  }
+  return true;
+}
+
+// Every strided input and every output of the call is mapped (see above).
+static bool all_mapped(const otx_grid* g, const otx_rays* o, int surfaces) {
+  uint64_t gp[6];
+  int64_t gs[6];
+  grid_fields(g, gp, gs);
+  for (int i = 0; i < 6; ++i)
+    if (gp[i] && gs[i] != 0 && !mapped_same(gp[i], g->count * 4)) return false;
+  uint64_t* op[12];
+  int sz[12];
+  out_fields(o, op, sz);
+  const int64_t planes = surfaces > 1 ? (int64_t)(surfaces - 1) * o->surface_stride + g->count
+                                      : g->count;
+  for (int i = 0; i < 12; ++i)
+    if (*op[i] && !mapped_same(*op[i], planes * sz[i])) return false;
+  return true;
+}
+
+static HostPlan plan_host(const otx_grid* g, const otx_rays* o, int surfaces, int64_t workspace) {
+  HostPlan p;
+  p.surfaces = surfaces;
+  const int64_t n = g->count;
+  int64_t chunk = (n + HOST_TARGET_CHUNKS - 1) / HOST_TARGET_CHUNKS;
+  chunk = (chunk + HOST_MIN_CHUNK - 1) / HOST_MIN_CHUNK * HOST_MIN_CHUNK;
+  if (chunk > n) chunk = n > 0 ? n : 1;
+  if (workspace >= 0) {
+    // shrink to what the given workspace holds
+    while (chunk > 1 && HOST_HEAD + HOST_SLOTS * slot_bytes(g, o, surfaces, chunk) > workspace)
+      chunk = chunk > 4096 ? chunk / 2 : chunk - 1;
+  }
+  p.chunk = chunk;
+  p.slot = slot_bytes(g, o, surfaces, chunk);
+  p.needed = HOST_HEAD + HOST_SLOTS * p.slot;
+  return p;
+}
+
 }  // namespace otx
 
 using namespace otx;
 
 extern "C" {
+
+int64_t otx_trace_grid_host_workspace(const otx_grid* in, const otx_rays* out, int32_t surfaces) {
+  if (!in || !out || in->count < 0 || surfaces < 1) return -1;
+  if (in->count > 0 && all_mapped(in, out, surfaces)) return HOST_HEAD;
+  return plan_host(in, out, surfaces, -1).needed;
+}
+
+otx_status otx_trace_grid_host(const otx_system* sys, const otx_grid* in, const otx_rays* out,
+                               const otx_image* image, const otx_launch* launch, void* workspace,
+                               int64_t workspace_bytes, void* stream) {
+  otx_status st = validate_system(sys);
+  if (st != OTX_OK) return st;
+  if (!in || !out || in->count < 0) return OTX_ERR_INVALID;
+  if (sys->input_mode != OTX_INPUT_GRID_INFINITY && sys->input_mode != OTX_INPUT_GRID_FINITE)
+    return OTX_ERR_INVALID;
+  if (in->count > 0 && (!in->wavelength || !in->field_x || !in->field_y || !in->pupil_x ||
+                        !in->pupil_y))
+    return OTX_ERR_INVALID;
+  uint64_t gp[6];
+  int64_t gs[6];
+  grid_fields(in, gp, gs);
+  for (int i = 0; i < 6; ++i)
+    if (gs[i] != 0 && gs[i] != 1) return OTX_ERR_INVALID;  // host arrays: contiguous or scalar
+  st = validate_image(sys, image);
+  if (st != OTX_OK) return st;
+  const bool acc = launch && launch->accumulate;
+  const int surfaces = acc ? sys->num_surfaces : 1;
+  if (acc && out->surface_stride < in->count) return OTX_ERR_INVALID;
+  const int64_t n = in->count;
+  if (n == 0) return OTX_OK;
+  if (!workspace || (reinterpret_cast<uintptr_t>(workspace) % HOST_ALIGN) != 0)
+    return OTX_ERR_INVALID;
+  if (launch && ((launch->rays_per_thread != 0 && launch->rays_per_thread != 1 &&
+                  launch->rays_per_thread != 2) ||
+                 launch->block_size < 0 || launch->block_size > 256 ||
+                 launch->block_size % 32 != 0))
+    return OTX_ERR_INVALID;
+  if (workspace_bytes < HOST_HEAD) return OTX_ERR_SIZE;
+  cudaStream_t cs = reinterpret_cast<cudaStream_t>(stream);
+  char* ws = reinterpret_cast<char*>(workspace);
+  float* head = reinterpret_cast<float*>(ws);
+#define OTX_CK(x) \
+  if ((x) != cudaSuccess) return OTX_ERR_CUDA
+  if (all_mapped(in, out, surfaces)) {
+    // the kernel reads and writes the host arrays in place; broadcast
+    // scalars go to the head so that no thread reads host memory for them
+    otx_grid g = *in;
+    uint64_t* gdst[6] = {&g.wavelength, &g.field_x, &g.field_y, &g.pupil_x, &g.pupil_y,
+                         &g.intensity};
+    for (int i = 0; i < 6; ++i) {
+      if (!gp[i] || gs[i] != 0) continue;
+      OTX_CK(cudaMemcpyAsync(head + i, reinterpret_cast<const void*>(gp[i]), 4,
+                             cudaMemcpyHostToDevice, cs));
+      *gdst[i] = reinterpret_cast<uint64_t>(head + i);
+    }
+    TraceArgs a;
+    memset(&a, 0, sizeof(a));
+    a.grid = g;
+    a.out = *out;
+    if (image) a.img = *image;
+    a.count = n;
+    return launch_trace(sys, sys->input_mode, a, launch, stream);
+  }
+  const HostPlan plan = plan_host(in, out, surfaces, workspace_bytes);
+  if (plan.needed > workspace_bytes || plan.chunk < 1) return OTX_ERR_SIZE;
+
+  std::lock_guard<std::mutex> lock(g_pipe_mu);
+  HostPipe* pp = nullptr;
+  st = host_pipe(&pp);
+  if (st != OTX_OK) return st;
+  HostPipe& P = *pp;
+  // the copies start after the caller's earlier work on its stream
+  OTX_CK(cudaEventRecord(P.start, cs));
+  OTX_CK(cudaStreamWaitEvent(P.in, P.start, 0));
+  OTX_CK(cudaStreamWaitEvent(P.out, P.start, 0));
+  // broadcast scalars into the head
+  for (int i = 0; i < 6; ++i)
+    if (gp[i] && gs[i] == 0)
+      OTX_CK(cudaMemcpyAsync(head + i, reinterpret_cast<const void*>(gp[i]), 4,
+                             cudaMemcpyHostToDevice, P.in));
+  uint64_t* op[12];
+  int osz[12];
+  out_fields(out, op, osz);
+  const int64_t nchunks = (n + plan.chunk - 1) / plan.chunk;
+  for (int64_t c = 0; c < nchunks; ++c) {
+    const int s = (int)(c % HOST_SLOTS);
+    const int64_t first = c * plan.chunk;
+    const int64_t cn = first + plan.chunk <= n ? plan.chunk : n - first;
+    char* slot = ws + HOST_HEAD + s * plan.slot;
+    // inputs: wait until the trace that last read this slot is done
+    if (c >= HOST_SLOTS) OTX_CK(cudaStreamWaitEvent(P.in, P.traced[s], 0));
+    otx_grid g = *in;
+    uint64_t* gdst[6] = {&g.wavelength, &g.field_x, &g.field_y, &g.pupil_x, &g.pupil_y,
+                         &g.intensity};
+    char* cur = slot;
+    for (int i = 0; i < 6; ++i) {
+      if (!gp[i]) continue;
+      if (gs[i] == 0) {
+        *gdst[i] = reinterpret_cast<uint64_t>(head + i);
+        continue;
+      }
+      OTX_CK(cudaMemcpyAsync(cur, reinterpret_cast<const float*>(gp[i]) + first, cn * 4,
+                             cudaMemcpyHostToDevice, P.in));
+      *gdst[i] = reinterpret_cast<uint64_t>(cur);
+      cur += align_up(plan.chunk * 4);
+    }
+    g.count = cn;
+    OTX_CK(cudaEventRecord(P.copied[s], P.in));
+    // outputs of this slot: the previous copy out of the slot must be done
+    otx_rays o = *out;
+    uint64_t* odst[12];
+    int dummy[12];
+    out_fields(&o, odst, dummy);
+    char* obase[12];
+    for (int i = 0; i < 12; ++i) {
+      obase[i] = nullptr;
+      if (!*op[i]) continue;
+      obase[i] = cur;
+      *odst[i] = reinterpret_cast<uint64_t>(cur);
+      cur += align_up(plan.chunk * osz[i] * (int64_t)surfaces);
+    }
+    o.count = cn;
+    o.surface_stride = acc ? plan.chunk : 0;
+    OTX_CK(cudaStreamWaitEvent(cs, P.copied[s], 0));
+    if (c >= HOST_SLOTS) OTX_CK(cudaStreamWaitEvent(cs, P.drained[s], 0));
+    TraceArgs a;
+    memset(&a, 0, sizeof(a));
+    a.grid = g;
+    a.out = o;
+    if (image) a.img = *image;
+    a.count = cn;
+    st = launch_trace(sys, sys->input_mode, a, launch, stream);
+    if (st != OTX_OK) return st;
+    OTX_CK(cudaEventRecord(P.traced[s], cs));
+    // copy out: one copy per field and surface plane (1-D copies: a 2-D
+    // copy into pageable memory was seen to land nothing on GB300)
+    OTX_CK(cudaStreamWaitEvent(P.out, P.traced[s], 0));
+    for (int i = 0; i < 12; ++i) {
+      if (!obase[i]) continue;
+      const size_t e = (size_t)osz[i];
+      for (int j = 0; j < surfaces; ++j) {
+        char* dst = reinterpret_cast<char*>(*op[i]) +
+                    ((size_t)j * (size_t)(acc ? out->surface_stride : 0) + (size_t)first) * e;
+        const char* src = obase[i] + (size_t)j * (size_t)plan.chunk * e;
+        OTX_CK(cudaMemcpyAsync(dst, src, (size_t)cn * e, cudaMemcpyDeviceToHost, P.out));
+      }
+    }
+    OTX_CK(cudaEventRecord(P.drained[s], P.out));
+  }
+  // the caller's stream continues once every copy has landed
+  OTX_CK(cudaEventRecord(P.end, P.out));
+  OTX_CK(cudaStreamWaitEvent(cs, P.end, 0));
+#undef OTX_CK
+  return OTX_OK;
+}
 
 int64_t otx_sizeof(int32_t which) {
   switch (which) {

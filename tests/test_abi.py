@@ -134,3 +134,42 @@ def test_collect_and_sag_validation(built_library):
     s.surfaces[0].sag_type = 42
     assert built_library.otx_sag_eval(ctypes.byref(s), 0, ctypes.byref(r), ctypes.byref(r),
                                       None) == L.ERR_UNSUPPORTED
+
+
+def test_host_trace_validation(built_library):
+    """otx_trace_grid_host rejects bad arguments before any device work."""
+    lib = built_library
+    s = _system()
+    x = (ctypes.c_float * 8)()
+    g = L.Grid()
+    g.count = 8
+    for k in ("wavelength", "field_x", "field_y", "pupil_x", "pupil_y"):
+        setattr(g, k, ctypes.addressof(x))
+    g.stride_wavelength = g.stride_field = g.stride_pupil = 1
+    out = L.Rays()
+    need = lib.otx_trace_grid_host_workspace(ctypes.byref(g), ctypes.byref(out), 1)
+    assert need > 0
+    assert lib.otx_trace_grid_host_workspace(ctypes.byref(g), ctypes.byref(out), 0) == -1
+
+    def call(grid, ws, nbytes, sys_=s, ln=None):
+        return lib.otx_trace_grid_host(ctypes.byref(sys_), ctypes.byref(grid), ctypes.byref(out),
+                                       None, ln, ws, nbytes, None)
+
+    # host input strides other than 0 and 1
+    g.stride_pupil = 2
+    assert call(g, 256, need) == L.ERR_INVALID
+    g.stride_pupil = 1
+    # no workspace, unaligned workspace, a workspace too small for one ray
+    assert call(g, None, need) == L.ERR_INVALID
+    assert call(g, 257, need) == L.ERR_INVALID
+    assert call(g, 256, 64) == L.ERR_SIZE
+    # a rays-input system, bad launch shape
+    s2 = _system()
+    s2.input_mode = L.INPUT_RAYS
+    assert call(g, 256, need, sys_=s2) == L.ERR_INVALID
+    ln = L.Launch()
+    ln.rays_per_thread = 3
+    assert call(g, 256, need, ln=ctypes.byref(ln)) == L.ERR_INVALID
+    # empty input: nothing to do, no device call
+    g.count = 0
+    assert call(g, None, 0) == L.OK
