@@ -216,12 +216,12 @@ def run_surrogate(args, rank: int, world: int) -> None:
     img = sg.traced(np.full(n_cfg, per_cfg), seed=7 + 1000 * rank, image=True, outputs=())
     total = img.total
     for _ in range(max(1, args.warmup)):
-        sg.image(img, chunk=131072)
+        sg.image(img, chunk=args.image_chunk or None, fused=args.image_path == "fused")
         img.run()
     torch.cuda.synchronize()
     e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     e0.record()
-    _, stats = sg.image(img, chunk=131072)
+    _, stats = sg.image(img, chunk=args.image_chunk or None, fused=args.image_path == "fused")
     e1.record()
     sim = img.images.clone()
     e2.record()
@@ -248,6 +248,7 @@ def run_surrogate(args, rank: int, world: int) -> None:
         "dtype": "bf16 (network), f32 (trace)",
         "data": "synthetic (seeded Philox rays on the device)",
         "config": {"workload": "spectrograph-surrogate", "configs": n_cfg,
+                   "image_path": args.image_path,
                    "train_rays": 50_000_000, "held_out_rays": 1_000_000, "image_rays": total,
                    "network": "9-256-256-256-256-3 SiLU, BF16 weights, FP32 accumulation"},
         "plain_trace": {"value": total * surfaces / (ms_plain * 1e-3), "ms": ms_plain},
@@ -284,6 +285,10 @@ def main() -> None:
     ap.add_argument("--workload", default="precision", choices=["precision", "surrogate"])
     ap.add_argument("--train-steps", type=int, default=6000)
     ap.add_argument("--image-rays", type=int, default=1_000_000_000)
+    ap.add_argument("--image-chunk", type=int, default=0,
+                    help="rays per call of the image simulation (0: the path's default)")
+    ap.add_argument("--image-path", default="fused", choices=["fused", "layers"],
+                    help="fused tensor-core kernel, or the network layer by layer")
     ap.add_argument("--rays-per-thread", type=int, default=0)
     args = ap.parse_args()
 
@@ -385,7 +390,7 @@ def main() -> None:
         res = system.rayfunction(
             wavelength=host["wavelength"], field=V(host["field_x"], host["field_y"]),
             pupil=V(host["pupil_x"], host["pupil_y"]), normalized_field=False,
-            normalized_pupil=False, image=True, launch=launch,
+            normalized_pupil=False, image=True, launch=launch, outputs=outputs,
         )
         dt = time.perf_counter() - t0
         if i > 0:

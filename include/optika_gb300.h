@@ -276,6 +276,23 @@ typedef struct otx_surrogate {
   float pad2_[2];
 } otx_surrogate;
 
+/* A BF16 MLP for the fused image simulation: num_hidden SiLU layers of
+ * `width` units between num_inputs inputs and num_outputs outputs.  Layer
+ * l (0 .. num_hidden; the last is the output layer) has weights w[l], bf16
+ * row-major [out x ld[l]] (16-byte aligned rows, ld a multiple of 8) and
+ * fp32 biases b[l].  No counterpart in the reference. */
+#define OTX_MLP_MAX_HIDDEN 6
+typedef struct otx_mlp {
+  int32_t num_inputs;
+  int32_t num_hidden;
+  int32_t width;
+  int32_t num_outputs;
+  uint64_t w[OTX_MLP_MAX_HIDDEN + 1];
+  int32_t ld[OTX_MLP_MAX_HIDDEN + 1];
+  int32_t pad_;
+  uint64_t b[OTX_MLP_MAX_HIDDEN + 1];
+} otx_mlp;
+
 typedef struct otx_launch {
   int32_t rays_per_thread; /* 1, 2 or 4; 0 = library default          */
   int32_t block_size;      /* threads per CTA; 0 = library default     */
@@ -288,7 +305,8 @@ typedef struct otx_launch {
 /* ABI self-description: sizes of the descriptor structs, for binding
  * checks.  `which`: 0 otx_system, 1 otx_surface, 2 otx_rays, 3 otx_grid,
  * 4 otx_image, 5 otx_launch, 6 otx_affine, 7 otx_sensor, 8 otx_layer,
- * 9 otx_stack, 10 otx_periodic_stack, 11 otx_batch, 12 otx_surrogate. */
+ * 9 otx_stack, 10 otx_periodic_stack, 11 otx_batch, 12 otx_surrogate,
+ * 13 otx_mlp. */
 int64_t otx_sizeof(int32_t which);
 int32_t otx_abi_version(void);
 const char* otx_status_string(otx_status s);
@@ -460,6 +478,28 @@ otx_status otx_surrogate_image(const otx_system* base, const otx_batch* batch,
                                const otx_surrogate* sg, int64_t first, int64_t count,
                                const float* y, int32_t ldy, const float* aux,
                                const otx_image* image, unsigned long long* stats, void* stream);
+
+/* Image simulation of rays [first, first + count) of a batch in one
+ * persistent tensor-core kernel: the rays are generated, the network (9
+ * inputs, hidden width 256, 3 outputs) runs layer after layer with its
+ * activations kept in shared memory and its accumulators in TMEM, and rays
+ * of trusted configurations with |logit| >= logit_band land at baseline +
+ * out_scale * output (binned if logit > 0); every other ray is queued and
+ * traced through base (with the batch's overrides) by a second kernel.
+ * Same results as otx_surrogate_pack + otx_gemm_bf16 per layer +
+ * otx_surrogate_image up to FP32 rounding.  `workspace` (device, 256-byte
+ * aligned, otx_surrogate_image_fused_workspace() bytes) holds the queue.
+ * Adds into the per-configuration images and stats[4] = {rays, traced,
+ * binned by the network, binned by the trace}; *err (device int) is set if
+ * a bounded wait gave up.  No counterpart in the reference. */
+otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* batch,
+                                     const otx_surrogate* sg, const otx_mlp* net,
+                                     int64_t first, int64_t count, const otx_image* image,
+                                     void* workspace, int64_t workspace_bytes,
+                                     unsigned long long* stats, int32_t* err, void* stream);
+/* Workspace bytes of otx_surrogate_image_fused for `count` rays; -1 for
+ * invalid arguments. */
+int64_t otx_surrogate_image_fused_workspace(const otx_batch* batch, int64_t count);
 
 /* Bin rays given in the sensor's local frame into count and flux images.
  * Replaces optika/sensors/_sensors.py:92-161 (ImagingSensor.collect, the

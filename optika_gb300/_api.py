@@ -336,6 +336,9 @@ def trace_grid(system, *, wavelength, field, pupil, intensity=None, accumulate: 
     CPU tensor inputs take the streamed host path (:func:`trace_grid_host`)
     and give CPU outputs; anything else is moved to the GPU and gives GPU
     tensors."""
+    bad = set(outputs) - set(OUTPUT_FIELDS)
+    if bad:
+        raise ValueError(f"unknown ray output fields {sorted(bad)}; known: {OUTPUT_FIELDS}")
     vals = [wavelength, field.x, field.y, pupil.x, pupil.y, intensity]
     if _is_host(vals):
         return trace_grid_host(system, wavelength=wavelength, field=field, pupil=pupil,

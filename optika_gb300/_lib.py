@@ -248,6 +248,22 @@ class Surrogate(ctypes.Structure):
     ]
 
 
+MLP_MAX_HIDDEN = 6
+
+
+class Mlp(ctypes.Structure):
+    _fields_ = [
+        ("num_inputs", i32),
+        ("num_hidden", i32),
+        ("width", i32),
+        ("num_outputs", i32),
+        ("w", u64 * (MLP_MAX_HIDDEN + 1)),
+        ("ld", i32 * (MLP_MAX_HIDDEN + 1)),
+        ("pad_", i32),
+        ("b", u64 * (MLP_MAX_HIDDEN + 1)),
+    ]
+
+
 class Launch(ctypes.Structure):
     _fields_ = [
         ("rays_per_thread", i32),
@@ -271,6 +287,7 @@ LAYOUT = {
     10: PeriodicStack,
     11: Batch,
     12: Surrogate,
+    13: Mlp,
 }
 
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "_lib" / "liboptika_gb300.so"
@@ -341,6 +358,11 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_surrogate_image.argtypes = [P(System), P(Batch), P(Surrogate), i64, i64, v, i32, v,
                                         P(Image), v, v]
     lib.otx_surrogate_image.restype = i32
+    lib.otx_surrogate_image_fused.argtypes = [P(System), P(Batch), P(Surrogate), P(Mlp), i64, i64,
+                                              P(Image), v, i64, v, v, v]
+    lib.otx_surrogate_image_fused.restype = i32
+    lib.otx_surrogate_image_fused_workspace.argtypes = [P(Batch), i64]
+    lib.otx_surrogate_image_fused_workspace.restype = i64
     lib.otx_collect.argtypes = [P(Sensor), P(Rays), P(Image), v]
     lib.otx_collect.restype = i32
     lib.otx_sag_eval.argtypes = [P(System), i32, P(Rays), P(Rays), v]

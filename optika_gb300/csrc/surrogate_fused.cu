@@ -1,0 +1,565 @@
+// Image simulation with the surrogate network in one persistent
+// tensor-core kernel, and the traced fallback of the rays it does not land.
+//
+// k_surrogate_fused: every CTA (one per SM) holds two 128-ray tiles in
+// flight.  For each tile, 8 epilogue warps generate the rays (Philox, as the
+// batched trace does), pack the 9 network inputs as BF16 straight into
+// shared memory in the 128-byte-swizzled K-major layout the tensor cores
+// read, and keep the quadratic baseline of the image position in
+// registers.  One thread issues every tcgen05.mma (M = 128, FP32
+// accumulators in TMEM, 256 columns per tile); another streams the weight
+// matrices from L2 by TMA through a ring of 16 KB stages (the output
+// layer's weights stay resident).  After each layer the tile's epilogue
+// warps read the accumulators with tcgen05.ld, add the bias, apply SiLU
+// (one tanh per value) and write the next layer's BF16 input back into the
+// tile's shared-memory operand, while the tensor cores run the other
+// tile's layer.  Activations never leave the SM.  After the output layer a
+// ray of a trusted configuration whose vignetting logit is at least the
+// band away from 0 lands at baseline + out_scale * network output (binned
+// into its configuration's image if the logit is positive); every other
+// ray is appended to its configuration's fallback list.
+//
+// k_surrogate_fallback traces the listed rays through the configuration's
+// surfaces (staged in shared memory per configuration) and bins them.
+//
+// Every mbarrier wait is bounded; a wait that gives up sets the error flag,
+// the CTA stops issuing work, lets its copies land and frees its TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "../../include/optika_gb300.h"
+#include "surrogate_common.cuh"
+#include "tc.cuh"
+
+namespace otx {
+
+constexpr int F_ROWS = 128;                          // rays per tile (MMA M)
+constexpr int F_WIDTH = 256;                         // hidden width
+constexpr int F_KC = 64;                             // K elements per 128-byte chunk
+constexpr int F_A_CHUNK = F_ROWS * F_KC * 2;         // 16 KB: one K chunk of a tile
+constexpr int F_A_BYTES = (F_WIDTH / F_KC) * F_A_CHUNK;  // 64 KB: a tile's operand
+constexpr int F_NH = 128;                            // weight rows (N) per stage
+constexpr int F_STAGE = F_NH * F_KC * 2;             // 16 KB
+constexpr int F_STAGES = 5;
+constexpr int F_OUT_N = 16;                          // output layer N (3 used)
+constexpr int F_WOUT_CHUNK = F_OUT_N * F_KC * 2;     // 2 KB
+constexpr int F_MAX_HIDDEN = OTX_MLP_MAX_HIDDEN;
+constexpr int F_EPI_WARPS = 8;                       // per tile slot
+constexpr int F_THREADS = 32 * (2 + 2 * F_EPI_WARPS);  // 576
+constexpr int F_BIAS_FLOATS = F_MAX_HIDDEN * F_WIDTH + F_OUT_N;
+constexpr size_t F_SMEM = 1024 + 2 * F_A_BYTES + F_STAGES * F_STAGE + (F_WIDTH / F_KC) * F_WOUT_CHUNK +
+                          F_BIAS_FLOATS * 4 + 256;
+
+struct FusedArgs {
+  otx_batch b;
+  otx_surrogate sg;
+  otx_sensor sensor;
+  otx_image img;
+  int64_t first, count;
+  int64_t num_pairs;      // ceil(ceil(count / 128) / 2)
+  int num_hidden;
+  const float* bias[OTX_MLP_MAX_HIDDEN + 1];
+  int32_t* list;          // [count]: fallback rays (offsets from first), per-config regions
+  uint32_t* list_count;   // [num_configs]
+  unsigned long long* stats;
+  int* err;
+};
+
+struct FusedMaps {
+  CUtensorMap w[OTX_MLP_MAX_HIDDEN];  // layer l weights [width x in_l], boxes 128 x 64
+  CUtensorMap out;                    // output layer [n_out x width], boxes 16 x 64
+};
+
+__device__ __forceinline__ bool aborted(volatile int* flag) { return *flag != 0; }
+
+// First list slot of configuration c's region: its first ray in [first, first + count).
+__device__ __forceinline__ int64_t list_region(const int64_t* offs, int c, int64_t first) {
+  const int64_t o = offs[c];
+  return (o > first ? o : first) - first;
+}
+
+__global__ void __launch_bounds__(F_THREADS, 1)
+    k_surrogate_fused(const __grid_constant__ FusedMaps maps, const __grid_constant__ FusedArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint8_t* sa = smem;                                   // 2 tiles x 64 KB
+  uint8_t* sw = sa + 2 * F_A_BYTES;                     // weight ring
+  uint8_t* swo = sw + F_STAGES * F_STAGE;               // output layer weights
+  float* hb = reinterpret_cast<float*>(swo + (F_WIDTH / F_KC) * F_WOUT_CHUNK);  // bias / 2
+  float* bout = hb + F_MAX_HIDDEN * F_WIDTH;
+  uint64_t* wfull = reinterpret_cast<uint64_t*>(bout + F_OUT_N);
+  uint64_t* wempty = wfull + F_STAGES;
+  uint64_t* afull = wempty + F_STAGES;   // [2]
+  uint64_t* accfull = afull + 2;         // [2]
+  uint64_t* woutfull = accfull + 2;
+  uint64_t* mmadone = woutfull + 1;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(mmadone + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int L = a.num_hidden;
+
+  // biases: hidden layers pre-halved (SiLU is evaluated on z / 2)
+  for (int i = tid; i < L * F_WIDTH; i += F_THREADS) hb[i] = 0.5f * a.bias[i / F_WIDTH][i % F_WIDTH];
+  if (tid < F_OUT_N) bout[tid] = tid < 3 ? a.bias[L][tid] : 0.f;
+  if (tid == 0) {
+    for (int s = 0; s < F_STAGES; ++s) {
+      mbar_init(&wfull[s], 1);
+      mbar_init(&wempty[s], 1);
+    }
+    for (int g = 0; g < 2; ++g) {
+      mbar_init(&afull[g], 32 * F_EPI_WARPS);
+      mbar_init(&accfull[g], 1);
+    }
+    mbar_init(woutfull, 1);
+    mbar_init(mmadone, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) tmem_alloc(tslot, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = *tslot;
+
+  if (warp == 0) {
+    // ---------------------------------------------------------- producer
+    if (lane == 0) {
+      int64_t k = 0;  // stage loads issued
+      mbar_expect_tx(woutfull, (F_WIDTH / F_KC) * F_WOUT_CHUNK);
+      for (int kc = 0; kc < F_WIDTH / F_KC; ++kc)
+        tma_load_2d(swo + kc * F_WOUT_CHUNK, &maps.out, kc * F_KC, 0, woutfull);
+      bool ok = true;
+      for (int64_t p = blockIdx.x; ok && p < a.num_pairs; p += gridDim.x) {
+        for (int l = 0; ok && l < L; ++l) {
+          const int nk = l == 0 ? 1 : F_WIDTH / F_KC;
+          for (int g = 0; ok && g < 2; ++g) {
+            for (int kc = 0; ok && kc < nk; ++kc) {
+              for (int nh = 0; nh < F_WIDTH / F_NH; ++nh) {
+                const int s = (int)(k % F_STAGES);
+                if (k >= F_STAGES &&
+                    (aborted(abort_flag) ||
+                     !mbar_wait(&wempty[s], (uint32_t)(((k / F_STAGES) - 1) & 1)))) {
+                  ok = false;
+                  break;
+                }
+                mbar_expect_tx(&wfull[s], F_STAGE);
+                tma_load_2d(sw + s * F_STAGE, &maps.w[l], kc * F_KC, nh * F_NH, &wfull[s]);
+                ++k;
+              }
+            }
+          }
+        }
+      }
+      if (!ok) {
+        *abort_flag = 1;
+        atomicExch(a.err, 1);
+      }
+      // let every copy land before the CTA's shared memory is released
+      for (int64_t j = k - F_STAGES > 0 ? k - F_STAGES : 0; j < k; ++j)
+        mbar_wait(&wfull[j % F_STAGES], (uint32_t)((j / F_STAGES) & 1));
+      mbar_wait(woutfull, 0);
+    }
+  } else if (warp == 1) {
+    // ---------------------------------------------------------- MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t ID_H = idesc_bf16(F_ROWS, F_NH);
+      constexpr uint32_t ID_O = idesc_bf16(F_ROWS, F_OUT_N);
+      int64_t k = 0;
+      uint32_t ap[2] = {0u, 0u};
+      bool ok = mbar_wait(woutfull, 0);
+      for (int64_t p = blockIdx.x; ok && p < a.num_pairs; p += gridDim.x) {
+        for (int l = 0; ok && l <= L; ++l) {
+          for (int g = 0; ok && g < 2; ++g) {
+            if (aborted(abort_flag) || !mbar_wait(&afull[g], ap[g])) {
+              ok = false;
+              break;
+            }
+            ap[g] ^= 1u;
+            tc_fence_after();
+            const uint32_t acc = tbase + (uint32_t)(g * F_WIDTH);
+            const uint8_t* A = sa + g * F_A_BYTES;
+            if (l < L) {
+              const int nk = l == 0 ? 1 : F_WIDTH / F_KC;
+              const int nkk = l == 0 ? 1 : F_KC / 16;  // layer 0: K = 16 (9 inputs, zero padded)
+              for (int kc = 0; ok && kc < nk; ++kc) {
+                const uint64_t ad = desc_sw128(A + kc * F_A_CHUNK);
+                for (int nh = 0; nh < F_WIDTH / F_NH; ++nh) {
+                  const int s = (int)(k % F_STAGES);
+                  if (!mbar_wait(&wfull[s], (uint32_t)((k / F_STAGES) & 1))) {
+                    ok = false;
+                    break;
+                  }
+                  tc_fence_after();
+                  const uint64_t bd = desc_sw128(sw + s * F_STAGE);
+                  for (int kk = 0; kk < nkk; ++kk)
+                    umma_bf16(acc + (uint32_t)(nh * F_NH), ad + 2 * kk, bd + 2 * kk, ID_H,
+                              (kc | kk) != 0);
+                  umma_commit(&wempty[s]);
+                  ++k;
+                }
+              }
+            } else {
+              for (int kc = 0; kc < F_WIDTH / F_KC; ++kc) {
+                const uint64_t ad = desc_sw128(A + kc * F_A_CHUNK);
+                const uint64_t bd = desc_sw128(swo + kc * F_WOUT_CHUNK);
+                for (int kk = 0; kk < F_KC / 16; ++kk)
+                  umma_bf16(acc, ad + 2 * kk, bd + 2 * kk, ID_O, (kc | kk) != 0);
+              }
+            }
+            if (ok) umma_commit(&accfull[g]);
+          }
+        }
+      }
+      if (!ok) {
+        *abort_flag = 1;
+        atomicExch(a.err, 1);
+      }
+      // every MMA issued so far has finished before TMEM is freed
+      umma_commit(mmadone);
+      mbar_wait(mmadone, 0);
+    }
+  } else {
+    // ---------------------------------------------------------- epilogue
+    const int g = (warp - 2) / F_EPI_WARPS;       // tile slot
+    const int lw = (warp - 2) % F_EPI_WARPS;
+    const int ch = lw / 4;                        // column half of the hidden layers
+    const int q = warp & 3;                       // TMEM lane quarter of this warp
+    const int row = q * 32 + lane;
+    uint8_t* A = sa + g * F_A_BYTES;
+    const uint32_t tacc = tbase + (uint32_t)(g * F_WIDTH) + ((uint32_t)(q * 32) << 16);
+    const int64_t* offs = reinterpret_cast<const int64_t*>(a.b.ray_offset);
+    const float* cin = reinterpret_cast<const float*>(a.sg.config_inputs);
+    const float* coef = reinterpret_cast<const float*>(a.sg.baseline);
+    const uint8_t* trusted = reinterpret_cast<const uint8_t*>(a.sg.trusted);
+    const bool bin = a.img.counts || a.img.flux;
+    uint32_t cp = 0u;  // accfull parity
+    unsigned long long n_rays = 0, n_net = 0, n_fb = 0;
+    bool ok = true;
+    for (int64_t p = blockIdx.x; ok && p < a.num_pairs; p += gridDim.x) {
+      const int64_t t = 2 * p + g;
+      const int64_t r = t * F_ROWS + row;  // offset of this row's ray from first
+      const bool valid = r < a.count;
+      int cfg = 0;
+      float bx = 0.f, by = 0.f, wl = 0.f;
+      if (ch == 0) {
+        // ---- rays and network inputs of this tile
+        float f[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) f[j] = 0.f;
+        if (valid) {
+          const int64_t gid = a.first + r;
+          cfg = config_of(offs, a.b.num_configs, gid);
+          const BatchInputs v = batch_inputs(a.b, cfg, gid - offs[cfg]);
+          ray_features(a.b, v, f);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) f[5 + j] = cin[cfg * 4 + j];
+          baseline_xy(coef + (int64_t)cfg * 2 * OTX_SURROGATE_NBASE, f, bx, by);
+          wl = v.wl;
+        }
+        uint32_t w[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) w[j] = pack_bf16x2(f[2 * j], f[2 * j + 1]);
+        uint8_t* rp = A + row * 128;
+        const int sx = row & 7;
+        *reinterpret_cast<uint4*>(rp + ((0 ^ sx) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
+        *reinterpret_cast<uint4*>(rp + ((1 ^ sx) << 4)) = make_uint4(w[4], w[5], w[6], w[7]);
+      }
+      fence_proxy_async_smem();
+      tc_fence_before();
+      mbar_arrive(&afull[g]);
+      // ---- hidden layers: TMEM -> bias, SiLU -> BF16 operand of the next layer
+      for (int l = 0; l < L; ++l) {
+        if (aborted(abort_flag) || !mbar_wait(&accfull[g], cp)) {
+          ok = false;
+          break;
+        }
+        cp ^= 1u;
+        tc_fence_after();
+        const float* hbl = hb + l * F_WIDTH;
+#pragma unroll 1
+        for (int blk = 0; blk < 4; ++blk) {
+          const int c0 = ch * 128 + blk * 32;
+          float v[32];
+          __syncwarp();
+          tmem_ld32(tacc + (uint32_t)c0, v);
+          uint32_t w[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const float2 bb = *reinterpret_cast<const float2*>(hbl + c0 + 2 * i);
+            const float h0 = fmaf(0.5f, v[2 * i], bb.x);
+            const float h1 = fmaf(0.5f, v[2 * i + 1], bb.y);
+            w[i] = pack_bf16x2(fmaf(h0, tanh_approx(h0), h0), fmaf(h1, tanh_approx(h1), h1));
+          }
+          uint8_t* rp = A + (c0 >> 6) * F_A_CHUNK + row * 128;
+          const int u0 = (c0 & 63) >> 3, sx = row & 7;
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            *reinterpret_cast<uint4*>(rp + (((u0 + j) ^ sx) << 4)) =
+                make_uint4(w[4 * j], w[4 * j + 1], w[4 * j + 2], w[4 * j + 3]);
+        }
+        fence_proxy_async_smem();
+        tc_fence_before();
+        mbar_arrive(&afull[g]);
+      }
+      if (!ok) break;
+      // ---- output layer: land, bin or queue for the trace
+      if (aborted(abort_flag) || !mbar_wait(&accfull[g], cp)) {
+        ok = false;
+        break;
+      }
+      cp ^= 1u;
+      tc_fence_after();
+      if (ch == 0) {
+        float v[16];
+        __syncwarp();
+        tmem_ld16(tacc, v);
+        const float y0 = v[0] + bout[0], y1 = v[1] + bout[1], s = v[2] + bout[2];
+        bool fb = false;
+        if (valid) {
+          ++n_rays;
+          const bool ok_cfg = trusted ? trusted[cfg] != 0 : true;
+          if (!ok_cfg || !(fabsf(s) >= a.sg.logit_band)) {  // NaN logits are traced too
+            fb = true;
+          } else if (s > 0.f && bin) {
+            Ray ray;
+            ray.px = fmaf(a.sg.out_scale, y0, bx);
+            ray.py = fmaf(a.sg.out_scale, y1, by);
+            ray.wl = wl;
+            ray.inten = 1.f;
+            ray.ok = true;
+            if (sensor_bin(a.sensor, ray) >= 0) ++n_net;
+            bin_ray(a.sensor, config_image(a.img, a.b.image_stride, cfg), ray);
+          }
+        }
+        // append to the configuration's list, one atomic per configuration and warp
+        const unsigned m = __ballot_sync(0xffffffffu, fb);
+        if (m) {
+          const unsigned same = __match_any_sync(0xffffffffu, fb ? cfg : -1);
+          const unsigned grp = same & m;
+          if (fb) {
+            const int leader = __ffs(grp) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(a.list_count + cfg, (uint32_t)__popc(grp));
+            base = __shfl_sync(grp, base, leader);
+            const uint32_t idx = base + __popc(grp & ((1u << lane) - 1u));
+            a.list[list_region(offs, cfg, a.first) + idx] = (int32_t)r;
+            ++n_fb;
+          }
+        }
+      }
+    }
+    if (!ok) {
+      *abort_flag = 1;
+      if (lane == 0) atomicExch(a.err, 1);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      n_rays += __shfl_xor_sync(0xffffffffu, n_rays, o);
+      n_net += __shfl_xor_sync(0xffffffffu, n_net, o);
+      n_fb += __shfl_xor_sync(0xffffffffu, n_fb, o);
+    }
+    if (lane == 0 && ch == 0) {
+      if (n_rays) atomicAdd(a.stats + 0, n_rays);
+      if (n_fb) atomicAdd(a.stats + 1, n_fb);
+      if (n_net) atomicAdd(a.stats + 2, n_net);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) tmem_dealloc(tbase, 512);
+}
+
+constexpr int FB_BLOCK = 256;
+
+struct FallbackArgs {
+  otx_batch b;
+  int64_t first, count;
+  const int32_t* list;
+  const uint32_t* list_count;
+  otx_image img;
+  unsigned long long* stats;
+};
+
+// Trace the queued rays: CTA (x, c) takes configuration c's list.
+template <class... Ks>
+__global__ void __launch_bounds__(FB_BLOCK)
+    k_surrogate_fallback(const __grid_constant__ otx_system sys,
+                         const __grid_constant__ FallbackArgs a) {
+  __shared__ otx_surface surf[OTX_MAX_SURFACES];
+  const int c = blockIdx.y, tid = threadIdx.x;
+  const int64_t* offs = reinterpret_cast<const int64_t*>(a.b.ray_offset);
+  const int64_t lo = list_region(offs, c, a.first);
+  const int64_t hi_ray = offs[c + 1] - a.first;
+  const int64_t cap = (hi_ray < a.count ? hi_ray : a.count) - lo;
+  int64_t n = a.list_count[c];
+  if (n > cap) n = cap > 0 ? cap : 0;
+  if (n == 0 || (int64_t)blockIdx.x * FB_BLOCK >= n) return;  // uniform over the CTA
+  const int words = sys.num_surfaces * (int)(sizeof(otx_surface) / 4);
+  const int* src = reinterpret_cast<const int*>(sys.surfaces);
+  int* dst = reinterpret_cast<int*>(surf);
+  for (int w = tid; w < words; w += FB_BLOCK) dst[w] = src[w];
+  __syncthreads();
+  const otx_surface* ov = reinterpret_cast<const otx_surface*>(a.b.overrides);
+  for (int j = 0; j < a.b.num_overrides; ++j) {
+    const int ow = (int)(sizeof(otx_surface) / 4);
+    const int* os = reinterpret_cast<const int*>(ov + (int64_t)c * a.b.num_overrides + j);
+    int* od = reinterpret_cast<int*>(surf + a.b.override_index[j]);
+    for (int w = tid; w < ow; w += FB_BLOCK) od[w] = os[w];
+  }
+  __syncthreads();
+  const otx_image img = config_image(a.img, a.b.image_stride, c);
+  const bool bin = img.counts || img.flux;
+  int binned = 0;
+  for (int64_t i = (int64_t)blockIdx.x * FB_BLOCK + tid; i < n; i += (int64_t)gridDim.x * FB_BLOCK) {
+    const int64_t gid = a.first + a.list[lo + i];
+    Ray ray;
+    batch_ray(a.b, c, gid - offs[c], ray);
+    propagate_all<Ks...>(sys, surf, ray);
+    if (bin) {
+      if (ray.ok && sensor_bin(sys.sensor, ray) >= 0) ++binned;
+      bin_ray(sys.sensor, img, ray);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) binned += __shfl_xor_sync(0xffffffffu, binned, o);
+  if ((tid & 31) == 0 && binned) atomicAdd(a.stats + 3, (unsigned long long)binned);
+}
+
+static int device_sms() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 132;
+}
+
+}  // namespace otx
+
+using namespace otx;
+
+extern "C" {
+
+int64_t otx_surrogate_image_fused_workspace(const otx_batch* batch, int64_t count) {
+  if (!batch || count < 0 || batch->num_configs < 1) return -1;
+  const int64_t list = (count * 4 + 255) / 256 * 256;
+  return list + ((int64_t)batch->num_configs * 4 + 255) / 256 * 256;
+}
+
+otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* batch,
+                                     const otx_surrogate* sg, const otx_mlp* net, int64_t first,
+                                     int64_t count, const otx_image* image, void* workspace,
+                                     int64_t workspace_bytes, unsigned long long* stats,
+                                     int32_t* err, void* stream) {
+  if (!base || !batch || !sg || !net || !stats || !err || first < 0 || count < 0)
+    return OTX_ERR_INVALID;
+  const otx_batch& b = *batch;
+  if (b.num_configs < 1 || !b.ray_offset || sg->num_configs != b.num_configs ||
+      !sg->config_inputs || !sg->baseline || !(sg->out_scale > 0.f))
+    return OTX_ERR_INVALID;
+  if (base->abi_version != OTX_ABI_VERSION || base->input_mode != OTX_INPUT_GRID_INFINITY)
+    return OTX_ERR_INVALID;
+  if (base->num_surfaces < 1 || base->num_surfaces > OTX_MAX_SURFACES) return OTX_ERR_SIZE;
+  if (!(base->flags & OTX_SYS_FLAG_FINAL_IDENTITY)) return OTX_ERR_UNSUPPORTED;
+  if (b.num_overrides < 0 || b.num_overrides > OTX_BATCH_MAX_OVERRIDES) return OTX_ERR_SIZE;
+  for (int j = 0; j < b.num_overrides; ++j)
+    if (b.override_index[j] < 0 || b.override_index[j] >= base->num_surfaces)
+      return OTX_ERR_INVALID;
+  if (b.num_overrides > 0 && !b.overrides) return OTX_ERR_INVALID;
+  // the network this kernel is built for: 9 inputs, hidden width 256, 3 outputs
+  if (net->num_hidden < 1 || net->num_hidden > OTX_MLP_MAX_HIDDEN || net->width != F_WIDTH ||
+      net->num_inputs != OTX_SURROGATE_NIN || net->num_outputs != 3)
+    return OTX_ERR_UNSUPPORTED;
+  const int L = net->num_hidden;
+  for (int l = 0; l <= L; ++l) {
+    if (!net->w[l] || !net->b[l] || (net->w[l] & 15) || net->ld[l] % 8) return OTX_ERR_INVALID;
+    const int in = l == 0 ? net->num_inputs : F_WIDTH;
+    if (net->ld[l] < in) return OTX_ERR_INVALID;
+  }
+  const bool bin = image && (image->counts || image->flux);
+  if (bin && (base->sensor.num_x < 1 || base->sensor.num_y < 1 || base->sensor.num_w < 1 ||
+              !(base->sensor.width_x > 0.f) || !(base->sensor.width_y > 0.f) ||
+              b.image_stride < base->sensor.num_w * base->sensor.num_x * base->sensor.num_y))
+    return OTX_ERR_INVALID;
+  if (count > 0x7fffffffLL) return OTX_ERR_SIZE;  // list entries are int32 offsets
+  const int64_t need = otx_surrogate_image_fused_workspace(batch, count);
+  if (!workspace || workspace_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255))
+    return OTX_ERR_INVALID;
+  if (count == 0) return OTX_OK;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+
+  FusedMaps maps;
+  memset(&maps, 0, sizeof(maps));
+  for (int l = 0; l < L; ++l) {
+    const int in = l == 0 ? net->num_inputs : F_WIDTH;
+    if (!make_map(&maps.w[l], reinterpret_cast<const void*>(net->w[l]), F_WIDTH, in, net->ld[l],
+                  F_NH))
+      return OTX_ERR_CUDA;
+  }
+  if (!make_map(&maps.out, reinterpret_cast<const void*>(net->w[L]), 3, F_WIDTH, net->ld[L],
+                F_OUT_N))
+    return OTX_ERR_CUDA;
+
+  otx_system sys = *base;
+  otx_sensor& S = sys.sensor;
+  S.inv_width_x = S.width_x > 0.f ? 1.f / S.width_x : 0.f;
+  S.inv_width_y = S.width_y > 0.f ? 1.f / S.width_y : 0.f;
+  S.inv_width_w = (S.w_hi > S.w_lo) ? (float)S.num_w / (S.w_hi - S.w_lo) : 0.f;
+
+  char* ws = reinterpret_cast<char*>(workspace);
+  int32_t* list = reinterpret_cast<int32_t*>(ws);
+  uint32_t* list_count = reinterpret_cast<uint32_t*>(ws + (count * 4 + 255) / 256 * 256);
+  if (cudaMemsetAsync(list_count, 0, (size_t)b.num_configs * 4, st) != cudaSuccess)
+    return OTX_ERR_CUDA;
+
+  FusedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.b = b;
+  a.sg = *sg;
+  a.sensor = S;
+  if (bin) a.img = *image;
+  a.first = first;
+  a.count = count;
+  const int64_t tiles = (count + F_ROWS - 1) / F_ROWS;
+  a.num_pairs = (tiles + 1) / 2;
+  a.num_hidden = L;
+  for (int l = 0; l <= L; ++l) a.bias[l] = reinterpret_cast<const float*>(net->b[l]);
+  a.list = list;
+  a.list_count = list_count;
+  a.stats = stats;
+  a.err = err;
+
+  static bool configured = false;
+  if (!configured) {
+    if (cudaFuncSetAttribute(k_surrogate_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)F_SMEM) != cudaSuccess)
+      return OTX_ERR_CUDA;
+    configured = true;
+  }
+  const int sms = device_sms();
+  const int64_t grid = a.num_pairs < sms ? a.num_pairs : sms;
+  k_surrogate_fused<<<(unsigned)grid, F_THREADS, F_SMEM, st>>>(maps, a);
+  if (cudaGetLastError() != cudaSuccess) return OTX_ERR_CUDA;
+
+  FallbackArgs f;
+  memset(&f, 0, sizeof(f));
+  f.b = b;
+  f.first = first;
+  f.count = count;
+  f.list = list;
+  f.list_count = list_count;
+  if (bin) f.img = *image;
+  f.stats = stats;
+  const int gx = (4 * sms + b.num_configs - 1) / b.num_configs;
+  const dim3 fgrid((unsigned)(gx > 0 ? gx : 1), (unsigned)b.num_configs);
+  if (shape_matches<BObject, BSphere, BGrating, BSensor>(sys))
+    k_surrogate_fallback<BObject, BSphere, BGrating, BSensor><<<fgrid, FB_BLOCK, 0, st>>>(sys, f);
+  else
+    k_surrogate_fallback<><<<fgrid, FB_BLOCK, 0, st>>>(sys, f);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -459,6 +459,7 @@ int64_t otx_sizeof(int32_t which) {
     case 10: return sizeof(otx_periodic_stack);
     case 11: return sizeof(otx_batch);
     case 12: return sizeof(otx_surrogate);
+    case 13: return sizeof(otx_mlp);
     default: return -1;
   }
 }

@@ -214,6 +214,19 @@ class MLP:
                                       1, b.shape[0], lr, beta1, beta2, eps, self.step_count, None, 0,
                                       None, 0, sh), "otx_adam")
 
+    def desc(self) -> L.Mlp:
+        """The network for the fused kernels: BF16 weights, FP32 biases."""
+        m = L.Mlp()
+        m.num_inputs = self.widths[0]
+        m.num_hidden = len(self.widths) - 2
+        m.width = self.widths[1]
+        m.num_outputs = self.widths[-1]
+        for l in range(len(self.w)):
+            m.w[l] = ptr(self.w16[l])
+            m.ld[l] = self.w16[l].shape[1]
+            m.b[l] = ptr(self.b[l])
+        return m
+
     def check_errors(self) -> None:
         if int(self.err.item()) != 0:
             raise RuntimeError("a tensor-core GEMM gave up waiting for its pipeline")
@@ -431,18 +444,39 @@ class RayMapSurrogate:
         self.trusted.copy_(t)
         return int(t.sum())
 
-    def image(self, bt, chunk: int = 131072):
+    def image(self, bt, chunk: int | None = None, fused: bool = True):
         """Sensor images of a batch (bt built with image=True): network for
         confidently classified rays of trusted configurations, plain trace
-        (same launch) for the rest.  Returns (images, stats[4] = rays, traced,
-        binned by the network, binned by the trace)."""
+        for the rest.  Returns (images, stats[4] = rays, traced, binned by
+        the network, binned by the trace).
+
+        ``fused`` (default): one persistent tensor-core kernel per call of
+        up to ``chunk`` rays (default 2**28) generates the rays, runs the
+        whole network on chip and bins, and a second kernel traces the rays
+        it queued (``otx_surrogate_image_fused``).  Otherwise the network
+        runs layer by layer (``otx_gemm_bf16``) over chunks of ``chunk``
+        rays (default 131072) with the activations in HBM."""
         if bt.images is None:
             raise ValueError("the batch needs image=True")
         bt.images.zero_()
         stats = torch.zeros(4, dtype=torch.int64, device=self.dev)
-        bufs = self.mlp.buffers(chunk, train=False)
         lib, sh = self.lib, stream_handle()
         total = bt.total
+        if fused:
+            chunk = chunk or (1 << 28)
+            net = self.mlp.desc()
+            for f in range(0, total, chunk):
+                rows = min(chunk, total - f)
+                need = int(lib.otx_surrogate_image_fused_workspace(ctypes.byref(bt.batch), rows))
+                ws = torch.empty(max(need, 256), dtype=torch.uint8, device=self.dev)
+                st = lib.otx_surrogate_image_fused(
+                    ctypes.byref(bt.lowering.sys), ctypes.byref(bt.batch), ctypes.byref(self.sg),
+                    ctypes.byref(net), f, rows, ctypes.byref(bt.img), ptr(ws), need, ptr(stats),
+                    ptr(self.mlp.err), sh)
+                L.check(st, "otx_surrogate_image_fused")
+            return bt.images, stats
+        chunk = chunk or 131072
+        bufs = self.mlp.buffers(chunk, train=False)
         for f in range(0, total, chunk):
             rows = min(chunk, total - f)
             self._pack(bt, f, rows, bufs)

@@ -76,18 +76,24 @@ class SequentialSystem:
         image: bool = False,
         wavelength_bins=None,
         launch: None | L.Launch = None,
+        outputs: None | Sequence[str] = None,
     ) -> RayFunctionArray:
         """Trace input rays through every surface; outputs in the system's
         frame, stacked over surfaces (leading axis) when ``accumulate``
         (optika/systems/_sequential.py:836-925).  ``image=True`` also bins
-        the rays on the sensor (``result.image = (counts, flux)``)."""
-        from ._api import trace_grid
+        the rays on the sensor (``result.image = (counts, flux)``).
+        ``outputs`` names the ray fields to return (``px py pz dx dy dz
+        wavelength intensity attenuation index_refraction unvignetted
+        opl``; default all); the others are ``None``.  CPU tensor inputs
+        give CPU outputs."""
+        from ._api import OUTPUT_FIELDS, trace_grid
 
         wl, fld, pup = self._grid(wavelength, field, pupil, normalized_field, normalized_pupil)
         res = trace_grid(
             self, wavelength=wl, field=fld, pupil=pup, intensity=intensity,
             accumulate=accumulate, final_local=False, image=image,
             wavelength_bins=wavelength_bins, launch=launch,
+            outputs=OUTPUT_FIELDS if outputs is None else tuple(outputs),
         )
         res.inputs = ObjectVectorArray(wavelength=wl, field=fld, pupil=pup)
         return res
@@ -103,16 +109,19 @@ class SequentialSystem:
         image: bool = False,
         wavelength_bins=None,
         launch: None | L.Launch = None,
+        outputs: None | Sequence[str] = None,
     ) -> RayFunctionArray:
         """Rays at the last surface in the sensor's local frame
-        (optika/systems/_sequential.py:927-988)."""
-        from ._api import trace_grid
+        (optika/systems/_sequential.py:927-988).  ``outputs`` as in
+        :meth:`raytrace`."""
+        from ._api import OUTPUT_FIELDS, trace_grid
 
         wl, fld, pup = self._grid(wavelength, field, pupil, normalized_field, normalized_pupil)
         res = trace_grid(
             self, wavelength=wl, field=fld, pupil=pup, intensity=intensity,
             accumulate=False, final_local=True, image=image,
             wavelength_bins=wavelength_bins, launch=launch,
+            outputs=OUTPUT_FIELDS if outputs is None else tuple(outputs),
         )
         res.inputs = ObjectVectorArray(wavelength=wl, field=fld, pupil=pup)
         return res

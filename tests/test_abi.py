@@ -173,3 +173,44 @@ def test_host_trace_validation(built_library):
     # empty input: nothing to do, no device call
     g.count = 0
     assert call(g, None, 0) == L.OK
+
+
+def test_fused_surrogate_validation(built_library):
+    """otx_surrogate_image_fused rejects bad arguments before any device work."""
+    lib = built_library
+    s = _system(4)
+    s.flags = L.SYS_FLAG_FINAL_IDENTITY
+    b = L.Batch()
+    b.num_configs = 2
+    b.ray_offset = 256
+    sg = L.Surrogate()
+    sg.num_configs = 2
+    sg.config_inputs = sg.baseline = 256
+    sg.out_scale = 0.005
+    net = L.Mlp()
+    net.num_inputs, net.num_hidden, net.width, net.num_outputs = 9, 4, 256, 3
+    for l in range(5):
+        net.w[l] = 4096 * (l + 1)
+        net.b[l] = 4096 * (l + 9)
+        net.ld[l] = 16 if l == 0 else 256
+    need = lib.otx_surrogate_image_fused_workspace(ctypes.byref(b), 1000)
+    assert need >= 4000 and need % 256 == 0
+    assert lib.otx_surrogate_image_fused_workspace(None, 10) == -1
+
+    def call(count=1000, ws=256, nbytes=need, net_=net, sys_=s):
+        return lib.otx_surrogate_image_fused(ctypes.byref(sys_), ctypes.byref(b), ctypes.byref(sg),
+                                             ctypes.byref(net_), 0, count, None, ws, nbytes,
+                                             256, 256, None)
+
+    assert call(count=0) == L.OK  # nothing to do, no device call
+    assert call(ws=None) == L.ERR_INVALID
+    assert call(ws=257) == L.ERR_INVALID
+    assert call(nbytes=need - 1) == L.ERR_INVALID
+    net2 = L.Mlp.from_buffer_copy(net)
+    net2.width = 128
+    assert call(net_=net2) == L.ERR_UNSUPPORTED
+    net2 = L.Mlp.from_buffer_copy(net)
+    net2.ld[1] = 100
+    assert call(net_=net2) == L.ERR_INVALID
+    s2 = _system(4)
+    assert call(sys_=s2) == L.ERR_UNSUPPORTED  # outputs must be in the sensor frame

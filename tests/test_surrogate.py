@@ -240,3 +240,64 @@ def test_training_gain_and_fallback_image(cuda):
     # the images agree pixel by pixel up to rays landing one pixel over
     diff = (sim.double() - ref.double()).abs().sum().item() / ref.sum().item()
     assert diff < 0.5, diff
+
+
+def _trained(num_configs=4, rays=100_000, steps=300, seed=5):
+    sg, systems, params = _surrogate(num_configs, seed=seed)
+    train = sg.traced(np.full(num_configs, rays), seed=seed + 36)
+    sg.fit_baseline(train)
+    sg.train(train, steps=steps, batch=16384, lr=2e-3, log_every=steps)
+    return sg, systems
+
+
+@pytest.mark.gpu
+def test_fused_image_matches_layer_path(cuda):
+    """The fused kernel (rays generated, network on chip, one launch plus the
+    traced fallback) against the layer-by-layer path (a GEMM per layer,
+    activations in HBM) on the same rays: the same network with the same
+    BF16 rounding points and the same SiLU, so the routing statistics and
+    the count images agree up to the few rays whose FP32 accumulation order
+    flips a rounding; flux images up to atomic order as well."""
+    import torch
+
+    sg, _ = _trained()
+    bt = sg.traced(np.array([70_001, 5_000, 130_007, 999]), seed=43, image=True, outputs=())
+    img_a, st_a = sg.image(bt, fused=False)
+    img_a, st_a = img_a.clone(), st_a.cpu().numpy()
+    img_b, st_b = sg.image(bt, fused=True)
+    torch.cuda.synchronize()
+    sg.mlp.check_errors()
+    st_b = st_b.cpu().numpy()
+    n = bt.total
+    assert st_a[0] == st_b[0] == n
+    assert abs(int(st_a[1]) - int(st_b[1])) <= max(2, n // 10000), (st_a, st_b)
+    assert abs(int(st_a[2] + st_a[3]) - int(st_b[2] + st_b[3])) <= max(2, n // 10000)
+    diff = (img_a.long() - img_b.long()).abs().sum().item()
+    assert diff <= max(4, n // 5000), (diff, st_a, st_b)
+    assert int(img_b.sum()) == int(st_b[2] + st_b[3])
+
+
+@pytest.mark.gpu
+def test_fused_image_chunks_and_untrusted(cuda):
+    """Calls over sub-ranges of the batch (first > 0, configurations split
+    between calls) add up to the single call; an untrusted configuration is
+    traced ray by ray, so its image equals the plain batched trace's."""
+    import torch
+
+    sg, _ = _trained()
+    bt = sg.traced(np.array([40_000, 3_001, 52_777, 10_000]), seed=47, image=True, outputs=())
+    one, st1 = sg.image(bt, fused=True)
+    one, st1 = one.clone(), st1.cpu().numpy()
+    many, st2 = sg.image(bt, chunk=17_000, fused=True)
+    torch.cuda.synchronize()
+    assert torch.equal(one, many)
+    assert np.array_equal(st1, st2.cpu().numpy())
+    # configuration 2 untrusted: all of its rays go to the trace
+    sg.trusted.copy_(torch.tensor([1, 1, 0, 1], dtype=torch.uint8))
+    img, st = sg.image(bt, fused=True)
+    img = img.clone()
+    bt.run()
+    torch.cuda.synchronize()
+    sg.mlp.check_errors()
+    assert torch.equal(img[2], bt.images[2])
+    assert int(st[1]) >= 52_777
