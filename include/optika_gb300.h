@@ -487,19 +487,23 @@ otx_status otx_surrogate_image(const otx_system* base, const otx_batch* batch,
  * out_scale * output (binned if logit > 0); every other ray is queued and
  * traced through base (with the batch's overrides) by a second kernel.
  * Same results as otx_surrogate_pack + otx_gemm_bf16 per layer +
- * otx_surrogate_image up to FP32 rounding.  `workspace` (device, 256-byte
- * aligned, otx_surrogate_image_fused_workspace() bytes) holds the queue.
- * Adds into the per-configuration images and stats[4] = {rays, traced,
- * binned by the network, binned by the trace}; *err (device int) is set if
- * a bounded wait gave up.  No counterpart in the reference. */
+ * otx_surrogate_image up to FP32 rounding.  `predict` (device float4
+ * [count], 16-byte aligned, or null) receives each ray's predicted
+ * position (mm) and logit; with predict and no image nothing is binned,
+ * queued or traced.  `workspace` (device, 256-byte aligned,
+ * otx_surrogate_image_fused_workspace() bytes) holds the queue.  Adds into
+ * the per-configuration images and stats[4] = {rays, traced, binned by the
+ * network, binned by the trace}; *err (device int) is set if a bounded wait
+ * gave up.  No counterpart in the reference. */
 otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* batch,
                                      const otx_surrogate* sg, const otx_mlp* net,
                                      int64_t first, int64_t count, const otx_image* image,
-                                     void* workspace, int64_t workspace_bytes,
+                                     float* predict, void* workspace, int64_t workspace_bytes,
                                      unsigned long long* stats, int32_t* err, void* stream);
-/* Workspace bytes of otx_surrogate_image_fused for `count` rays; -1 for
- * invalid arguments. */
-int64_t otx_surrogate_image_fused_workspace(const otx_batch* batch, int64_t count);
+/* Workspace bytes of otx_surrogate_image_fused for `count` rays of this
+ * batch and network; -1 for invalid arguments. */
+int64_t otx_surrogate_image_fused_workspace(const otx_batch* batch, const otx_mlp* net,
+                                            int64_t count);
 
 /* Bin rays given in the sensor's local frame into count and flux images.
  * Replaces optika/sensors/_sensors.py:92-161 (ImagingSensor.collect, the

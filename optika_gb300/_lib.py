@@ -359,9 +359,9 @@ def _declare(lib: ctypes.CDLL) -> None:
                                         P(Image), v, v]
     lib.otx_surrogate_image.restype = i32
     lib.otx_surrogate_image_fused.argtypes = [P(System), P(Batch), P(Surrogate), P(Mlp), i64, i64,
-                                              P(Image), v, i64, v, v, v]
+                                              P(Image), v, v, i64, v, v, v]
     lib.otx_surrogate_image_fused.restype = i32
-    lib.otx_surrogate_image_fused_workspace.argtypes = [P(Batch), i64]
+    lib.otx_surrogate_image_fused_workspace.argtypes = [P(Batch), P(Mlp), i64]
     lib.otx_surrogate_image_fused_workspace.restype = i64
     lib.otx_collect.argtypes = [P(Sensor), P(Rays), P(Image), v]
     lib.otx_collect.restype = i32

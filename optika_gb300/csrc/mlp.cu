@@ -207,9 +207,12 @@ __global__ void __launch_bounds__(128, 1)
       float r[16];
       if (EPI == OTX_EPI_SILU_BF16) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          v[i] += (g.bias && i < valid) ? g.bias[c + i] : 0.f;
-          r[i] = silu(v[i]);
+        for (int i = 0; i < 16; ++i) v[i] += (g.bias && i < valid) ? g.bias[c + i] : 0.f;
+#pragma unroll
+        for (int i = 0; i < 16; i += 2) {
+          const uint32_t w = silu2_bf16(0.5f * v[i], 0.5f * v[i + 1]);
+          r[i] = __uint_as_float(w << 16);
+          r[i + 1] = __uint_as_float(w & 0xffff0000u);
         }
         if (g.z) store16_bf16(g.z + o, v, valid, vec);
       } else {  // DSILU: dZ = dH silu'(z), silu'(z) = s (1 + z (1 - s)), s = sigmoid(z)

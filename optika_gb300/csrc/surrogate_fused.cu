@@ -1,19 +1,21 @@
 // Image simulation with the surrogate network in one persistent
 // tensor-core kernel, and the traced fallback of the rays it does not land.
 //
-// k_surrogate_fused: every CTA (one per SM) holds two 128-ray tiles in
-// flight.  For each tile, 8 epilogue warps generate the rays (Philox, as the
+// k_surrogate_fused: every CTA (one per SM) runs two 128-ray tiles side by
+// side.  For each tile, 8 epilogue warps generate the rays (Philox, as the
 // batched trace does), pack the 9 network inputs as BF16 straight into
 // shared memory in the 128-byte-swizzled K-major layout the tensor cores
 // read, and keep the quadratic baseline of the image position in
-// registers.  One thread issues every tcgen05.mma (M = 128, FP32
+// registers.  One thread issues every tcgen05.mma (M = 128, N = 256, FP32
 // accumulators in TMEM, 256 columns per tile); another streams the weight
-// matrices from L2 by TMA through a ring of 16 KB stages (the output
-// layer's weights stay resident).  After each layer the tile's epilogue
-// warps read the accumulators with tcgen05.ld, add the bias, apply SiLU
-// (one tanh per value) and write the next layer's BF16 input back into the
-// tile's shared-memory operand, while the tensor cores run the other
-// tile's layer.  Activations never leave the SM.  After the output layer a
+// matrices from L2 by TMA through a ring of 32 KB stages (the output
+// layer's weights stay resident).  Each weight stage feeds both tiles'
+// MMAs, so a weight byte fetched from L2 serves 256 rays.  After each layer
+// the tiles' epilogue warps read the accumulators with tcgen05.ld, add the
+// bias, apply SiLU (packed BF16 tanh and FMA, one MUFU operation per two
+// values) and write the next layer's BF16 input back into the tile's
+// shared-memory operand.  Activations never
+// leave the SM.  After the output layer a
 // ray of a trusted configuration whose vignetting logit is at least the
 // band away from 0 lands at baseline + out_scale * network output (binned
 // into its configuration's image if the logit is positive); every other
@@ -41,9 +43,9 @@ constexpr int F_WIDTH = 256;                         // hidden width
 constexpr int F_KC = 64;                             // K elements per 128-byte chunk
 constexpr int F_A_CHUNK = F_ROWS * F_KC * 2;         // 16 KB: one K chunk of a tile
 constexpr int F_A_BYTES = (F_WIDTH / F_KC) * F_A_CHUNK;  // 64 KB: a tile's operand
-constexpr int F_NH = 128;                            // weight rows (N) per stage
-constexpr int F_STAGE = F_NH * F_KC * 2;             // 16 KB
-constexpr int F_STAGES = 5;
+constexpr int F_NH = 256;                            // weight rows (N) per stage
+constexpr int F_STAGE = F_NH * F_KC * 2;             // 32 KB
+constexpr int F_STAGES = 2;
 constexpr int F_OUT_N = 16;                          // output layer N (3 used)
 constexpr int F_WOUT_CHUNK = F_OUT_N * F_KC * 2;     // 2 KB
 constexpr int F_MAX_HIDDEN = OTX_MLP_MAX_HIDDEN;
@@ -66,10 +68,11 @@ struct FusedArgs {
   uint32_t* list_count;   // [num_configs]
   unsigned long long* stats;
   int* err;
+  float4* predict;        // [count] or null: {x, y, logit, 0}, position in mm
 };
 
 struct FusedMaps {
-  CUtensorMap w[OTX_MLP_MAX_HIDDEN];  // layer l weights [width x in_l], boxes 128 x 64
+  CUtensorMap w[OTX_MLP_MAX_HIDDEN];  // layer l weights [width x in_l], boxes 256 x 64
   CUtensorMap out;                    // output layer [n_out x width], boxes 16 x 64
 };
 
@@ -79,6 +82,27 @@ __device__ __forceinline__ bool aborted(volatile int* flag) { return *flag != 0;
 __device__ __forceinline__ int64_t list_region(const int64_t* offs, int c, int64_t first) {
   const int64_t o = offs[c];
   return (o > first ? o : first) - first;
+}
+
+// One block of 32 accumulator columns [c0, c0 + 32) of a row: bias, SiLU,
+// BF16, stored into the row's 128-byte-swizzled operand (four 16-byte
+// units, each written as soon as it is packed).
+__device__ __forceinline__ void epilogue_block(const uint32_t r[32], const float* hbl, uint8_t* A,
+                                               int c0, int row) {
+  uint8_t* rp = A + (c0 >> 6) * F_A_CHUNK + row * 128;
+  const int u0 = (c0 & 63) >> 3, sx = row & 7;
+  const float* v = reinterpret_cast<const float*>(r);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float4 b0 = *reinterpret_cast<const float4*>(hbl + c0 + 8 * j);
+    const float4 b1 = *reinterpret_cast<const float4*>(hbl + c0 + 8 * j + 4);
+    uint4 w;
+    w.x = silu2_bf16(fmaf(0.5f, v[8 * j + 0], b0.x), fmaf(0.5f, v[8 * j + 1], b0.y));
+    w.y = silu2_bf16(fmaf(0.5f, v[8 * j + 2], b0.z), fmaf(0.5f, v[8 * j + 3], b0.w));
+    w.z = silu2_bf16(fmaf(0.5f, v[8 * j + 4], b1.x), fmaf(0.5f, v[8 * j + 5], b1.y));
+    w.w = silu2_bf16(fmaf(0.5f, v[8 * j + 6], b1.z), fmaf(0.5f, v[8 * j + 7], b1.w));
+    *reinterpret_cast<uint4*>(rp + (((u0 + j) ^ sx) << 4)) = w;
+  }
 }
 
 __global__ void __launch_bounds__(F_THREADS, 1)
@@ -137,21 +161,17 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       for (int64_t p = blockIdx.x; ok && p < a.num_pairs; p += gridDim.x) {
         for (int l = 0; ok && l < L; ++l) {
           const int nk = l == 0 ? 1 : F_WIDTH / F_KC;
-          for (int g = 0; ok && g < 2; ++g) {
-            for (int kc = 0; ok && kc < nk; ++kc) {
-              for (int nh = 0; nh < F_WIDTH / F_NH; ++nh) {
-                const int s = (int)(k % F_STAGES);
-                if (k >= F_STAGES &&
-                    (aborted(abort_flag) ||
-                     !mbar_wait(&wempty[s], (uint32_t)(((k / F_STAGES) - 1) & 1)))) {
-                  ok = false;
-                  break;
-                }
-                mbar_expect_tx(&wfull[s], F_STAGE);
-                tma_load_2d(sw + s * F_STAGE, &maps.w[l], kc * F_KC, nh * F_NH, &wfull[s]);
-                ++k;
-              }
+          for (int kc = 0; kc < nk; ++kc) {
+            const int s = (int)(k % F_STAGES);
+            if (k >= F_STAGES &&
+                (aborted(abort_flag) ||
+                 !mbar_wait(&wempty[s], (uint32_t)(((k / F_STAGES) - 1) & 1)))) {
+              ok = false;
+              break;
             }
+            mbar_expect_tx(&wfull[s], F_STAGE);
+            tma_load_2d(sw + s * F_STAGE, &maps.w[l], kc * F_KC, 0, &wfull[s]);
+            ++k;
           }
         }
       }
@@ -174,44 +194,50 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       bool ok = mbar_wait(woutfull, 0);
       for (int64_t p = blockIdx.x; ok && p < a.num_pairs; p += gridDim.x) {
         for (int l = 0; ok && l <= L; ++l) {
+          // both tiles' inputs of this layer are in shared memory
           for (int g = 0; ok && g < 2; ++g) {
             if (aborted(abort_flag) || !mbar_wait(&afull[g], ap[g])) {
               ok = false;
               break;
             }
             ap[g] ^= 1u;
-            tc_fence_after();
-            const uint32_t acc = tbase + (uint32_t)(g * F_WIDTH);
-            const uint8_t* A = sa + g * F_A_BYTES;
-            if (l < L) {
-              const int nk = l == 0 ? 1 : F_WIDTH / F_KC;
-              const int nkk = l == 0 ? 1 : F_KC / 16;  // layer 0: K = 16 (9 inputs, zero padded)
-              for (int kc = 0; ok && kc < nk; ++kc) {
-                const uint64_t ad = desc_sw128(A + kc * F_A_CHUNK);
-                for (int nh = 0; nh < F_WIDTH / F_NH; ++nh) {
-                  const int s = (int)(k % F_STAGES);
-                  if (!mbar_wait(&wfull[s], (uint32_t)((k / F_STAGES) & 1))) {
-                    ok = false;
-                    break;
-                  }
-                  tc_fence_after();
-                  const uint64_t bd = desc_sw128(sw + s * F_STAGE);
-                  for (int kk = 0; kk < nkk; ++kk)
-                    umma_bf16(acc + (uint32_t)(nh * F_NH), ad + 2 * kk, bd + 2 * kk, ID_H,
-                              (kc | kk) != 0);
-                  umma_commit(&wempty[s]);
-                  ++k;
-                }
+          }
+          if (!ok) break;
+          tc_fence_after();
+          if (l < L) {
+            const int nk = l == 0 ? 1 : F_WIDTH / F_KC;
+            const int nkk = l == 0 ? 1 : F_KC / 16;  // layer 0: K = 16 (9 inputs, zero padded)
+            for (int kc = 0; kc < nk; ++kc) {
+              const int s = (int)(k % F_STAGES);
+              if (!mbar_wait(&wfull[s], (uint32_t)((k / F_STAGES) & 1))) {
+                ok = false;
+                break;
               }
-            } else {
+              tc_fence_after();
+              const uint64_t bd = desc_sw128(sw + s * F_STAGE);
+              for (int g = 0; g < 2; ++g) {
+                const uint64_t ad = desc_sw128(sa + g * F_A_BYTES + kc * F_A_CHUNK);
+                const uint32_t acc = tbase + (uint32_t)(g * F_WIDTH);
+                for (int kk = 0; kk < nkk; ++kk)
+                  umma_bf16(acc, ad + 2 * kk, bd + 2 * kk, ID_H, (kc | kk) != 0);
+              }
+              umma_commit(&wempty[s]);
+              ++k;
+            }
+          } else {
+            for (int g = 0; g < 2; ++g) {
+              const uint32_t acc = tbase + (uint32_t)(g * F_WIDTH);
               for (int kc = 0; kc < F_WIDTH / F_KC; ++kc) {
-                const uint64_t ad = desc_sw128(A + kc * F_A_CHUNK);
+                const uint64_t ad = desc_sw128(sa + g * F_A_BYTES + kc * F_A_CHUNK);
                 const uint64_t bd = desc_sw128(swo + kc * F_WOUT_CHUNK);
                 for (int kk = 0; kk < F_KC / 16; ++kk)
                   umma_bf16(acc, ad + 2 * kk, bd + 2 * kk, ID_O, (kc | kk) != 0);
               }
             }
-            if (ok) umma_commit(&accfull[g]);
+          }
+          if (ok) {
+            umma_commit(&accfull[0]);
+            umma_commit(&accfull[1]);
           }
         }
       }
@@ -281,27 +307,22 @@ __global__ void __launch_bounds__(F_THREADS, 1)
         cp ^= 1u;
         tc_fence_after();
         const float* hbl = hb + l * F_WIDTH;
-#pragma unroll 1
-        for (int blk = 0; blk < 4; ++blk) {
-          const int c0 = ch * 128 + blk * 32;
-          float v[32];
-          __syncwarp();
-          tmem_ld32(tacc + (uint32_t)c0, v);
-          uint32_t w[16];
-#pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const float2 bb = *reinterpret_cast<const float2*>(hbl + c0 + 2 * i);
-            const float h0 = fmaf(0.5f, v[2 * i], bb.x);
-            const float h1 = fmaf(0.5f, v[2 * i + 1], bb.y);
-            w[i] = pack_bf16x2(fmaf(h0, tanh_approx(h0), h0), fmaf(h1, tanh_approx(h1), h1));
-          }
-          uint8_t* rp = A + (c0 >> 6) * F_A_CHUNK + row * 128;
-          const int u0 = (c0 & 63) >> 3, sx = row & 7;
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-            *reinterpret_cast<uint4*>(rp + (((u0 + j) ^ sx) << 4)) =
-                make_uint4(w[4 * j], w[4 * j + 1], w[4 * j + 2], w[4 * j + 3]);
-        }
+        // four blocks of 32 columns; the TMEM load of block b + 1 is in
+        // flight while block b is converted
+        uint32_t ra[32], rb[32];
+        __syncwarp();
+        tmem_ld32_start(tacc + (uint32_t)(ch * 128), ra);
+        tmem_wait32(ra);
+        tmem_ld32_start(tacc + (uint32_t)(ch * 128 + 32), rb);
+        epilogue_block(ra, hbl, A, ch * 128, row);
+        tmem_wait32(rb);
+        tmem_ld32_start(tacc + (uint32_t)(ch * 128 + 64), ra);
+        epilogue_block(rb, hbl, A, ch * 128 + 32, row);
+        tmem_wait32(ra);
+        tmem_ld32_start(tacc + (uint32_t)(ch * 128 + 96), rb);
+        epilogue_block(ra, hbl, A, ch * 128 + 64, row);
+        tmem_wait32(rb);
+        epilogue_block(rb, hbl, A, ch * 128 + 96, row);
         fence_proxy_async_smem();
         tc_fence_before();
         mbar_arrive(&afull[g]);
@@ -320,12 +341,15 @@ __global__ void __launch_bounds__(F_THREADS, 1)
         tmem_ld16(tacc, v);
         const float y0 = v[0] + bout[0], y1 = v[1] + bout[1], s = v[2] + bout[2];
         bool fb = false;
-        if (valid) {
+        if (valid && a.predict)
+          a.predict[r] = make_float4(fmaf(a.sg.out_scale, y0, bx), fmaf(a.sg.out_scale, y1, by), s,
+                                     0.f);
+        if (valid && bin) {
           ++n_rays;
           const bool ok_cfg = trusted ? trusted[cfg] != 0 : true;
           if (!ok_cfg || !(fabsf(s) >= a.sg.logit_band)) {  // NaN logits are traced too
             fb = true;
-          } else if (s > 0.f && bin) {
+          } else if (s > 0.f) {
             Ray ray;
             ray.px = fmaf(a.sg.out_scale, y0, bx);
             ray.py = fmaf(a.sg.out_scale, y1, by);
@@ -443,19 +467,20 @@ using namespace otx;
 
 extern "C" {
 
-int64_t otx_surrogate_image_fused_workspace(const otx_batch* batch, int64_t count) {
-  if (!batch || count < 0 || batch->num_configs < 1) return -1;
-  const int64_t list = (count * 4 + 255) / 256 * 256;
-  return list + ((int64_t)batch->num_configs * 4 + 255) / 256 * 256;
+int64_t otx_surrogate_image_fused_workspace(const otx_batch* batch, const otx_mlp* net,
+                                            int64_t count) {
+  if (!batch || !net || count < 0 || batch->num_configs < 1) return -1;
+  return (count * 4 + 255) / 256 * 256 + ((int64_t)batch->num_configs * 4 + 255) / 256 * 256;
 }
 
 otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* batch,
                                      const otx_surrogate* sg, const otx_mlp* net, int64_t first,
-                                     int64_t count, const otx_image* image, void* workspace,
-                                     int64_t workspace_bytes, unsigned long long* stats,
-                                     int32_t* err, void* stream) {
+                                     int64_t count, const otx_image* image, float* predict,
+                                     void* workspace, int64_t workspace_bytes,
+                                     unsigned long long* stats, int32_t* err, void* stream) {
   if (!base || !batch || !sg || !net || !stats || !err || first < 0 || count < 0)
     return OTX_ERR_INVALID;
+  if (reinterpret_cast<uintptr_t>(predict) & 15) return OTX_ERR_INVALID;
   const otx_batch& b = *batch;
   if (b.num_configs < 1 || !b.ray_offset || sg->num_configs != b.num_configs ||
       !sg->config_inputs || !sg->baseline || !(sg->out_scale > 0.f))
@@ -485,14 +510,19 @@ otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* ba
               b.image_stride < base->sensor.num_w * base->sensor.num_x * base->sensor.num_y))
     return OTX_ERR_INVALID;
   if (count > 0x7fffffffLL) return OTX_ERR_SIZE;  // list entries are int32 offsets
-  const int64_t need = otx_surrogate_image_fused_workspace(batch, count);
+  const int64_t need = otx_surrogate_image_fused_workspace(batch, net, count);
   if (!workspace || workspace_bytes < need || (reinterpret_cast<uintptr_t>(workspace) & 255))
     return OTX_ERR_INVALID;
   if (count == 0) return OTX_OK;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
 
+  // workspace: fallback list, per-configuration counts
+  char* ws = reinterpret_cast<char*>(workspace);
+  int32_t* list = reinterpret_cast<int32_t*>(ws);
+  uint32_t* list_count = reinterpret_cast<uint32_t*>(ws + (count * 4 + 255) / 256 * 256);
   FusedMaps maps;
   memset(&maps, 0, sizeof(maps));
+  const int sms = device_sms();
   for (int l = 0; l < L; ++l) {
     const int in = l == 0 ? net->num_inputs : F_WIDTH;
     if (!make_map(&maps.w[l], reinterpret_cast<const void*>(net->w[l]), F_WIDTH, in, net->ld[l],
@@ -509,9 +539,6 @@ otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* ba
   S.inv_width_y = S.width_y > 0.f ? 1.f / S.width_y : 0.f;
   S.inv_width_w = (S.w_hi > S.w_lo) ? (float)S.num_w / (S.w_hi - S.w_lo) : 0.f;
 
-  char* ws = reinterpret_cast<char*>(workspace);
-  int32_t* list = reinterpret_cast<int32_t*>(ws);
-  uint32_t* list_count = reinterpret_cast<uint32_t*>(ws + (count * 4 + 255) / 256 * 256);
   if (cudaMemsetAsync(list_count, 0, (size_t)b.num_configs * 4, st) != cudaSuccess)
     return OTX_ERR_CUDA;
 
@@ -531,6 +558,7 @@ otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* ba
   a.list_count = list_count;
   a.stats = stats;
   a.err = err;
+  a.predict = reinterpret_cast<float4*>(predict);
 
   static bool configured = false;
   if (!configured) {
@@ -539,10 +567,10 @@ otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* ba
       return OTX_ERR_CUDA;
     configured = true;
   }
-  const int sms = device_sms();
   const int64_t grid = a.num_pairs < sms ? a.num_pairs : sms;
   k_surrogate_fused<<<(unsigned)grid, F_THREADS, F_SMEM, st>>>(maps, a);
   if (cudaGetLastError() != cudaSuccess) return OTX_ERR_CUDA;
+  if (!bin) return OTX_OK;  // predictions only: nothing was queued
 
   FallbackArgs f;
   memset(&f, 0, sizeof(f));

@@ -28,10 +28,13 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+// One potentially blocking test of the phase of the given parity: the
+// hardware suspends the thread until the phase completes or a system
+// time limit passes.
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
       "selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
       : "r"(smem_u32(bar)), "r"(parity)
@@ -39,13 +42,14 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait for the phase of the given parity: false after ~1 s.
+// Bounded wait for the phase of the given parity: false after about 2^31
+// SM clock cycles (about one second).
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int i = 0; i < (1 << 24); ++i) {
-    if (mbar_test(bar, parity)) return true;
-    if (i > 32) __nanosleep(64);
-  }
-  return false;
+  if (mbar_try(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try(bar, parity))
+    if (clock64() - t0 > (1LL << 31)) return false;
+  return true;
 }
 
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
@@ -158,6 +162,36 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float v[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Start loading 32 FP32 columns of this warp's TMEM lanes into r; the
+// registers are valid only after tmem_wait32(r).
+__device__ __forceinline__ void tmem_ld32_start(uint32_t taddr, uint32_t r[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+}
+
+// Wait for this thread's outstanding TMEM loads; r (the registers of the
+// last one) is marked as written here so that no use moves above the wait.
+__device__ __forceinline__ void tmem_wait32(uint32_t r[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]),
+                 "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
+                 "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]),
+                 "+r"(r[30]), "+r"(r[31])
+               :
+               : "memory");
+}
+
 // Packed bf16 pair from two floats (round to nearest even).
 __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
   __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
@@ -176,10 +210,17 @@ __device__ __forceinline__ float sigmoid_tanh(float z) {
   return fmaf(0.5f, tanh_approx(0.5f * z), 0.5f);
 }
 
-// SiLU z s(z), written as h + h tanh(h) with h = z / 2: one MUFU, two FMA.
-__device__ __forceinline__ float silu(float z) {
-  const float h = 0.5f * z;
-  return fmaf(h, tanh_approx(h), h);
+// SiLU z s(z), written as h + h tanh(h) with h = z / 2, for a pair of
+// pre-activations given as h0, h1 (already halved): h is rounded to BF16,
+// and tanh (one MUFU operation for both) and the FMA run in packed BF16
+// arithmetic; the result is the packed BF16 pair.  Every SiLU of the
+// network, in training and in inference, is this function.
+__device__ __forceinline__ uint32_t silu2_bf16(float h0, float h1) {
+  const uint32_t h = pack_bf16x2(h0, h1);
+  uint32_t t, o;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(h));
+  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(o) : "r"(h), "r"(t), "r"(h));
+  return o;
 }
 
 // ---------------------------------------------------------------- host

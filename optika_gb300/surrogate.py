@@ -316,8 +316,11 @@ class RayMapSurrogate:
                                 -1).double()
                 ata[c] += F.T @ F
                 aty[c] += F.T @ y
-        reg = 1e-9 * torch.eye(L.SURROGATE_NBASE, dtype=torch.float64, device=self.dev)
-        sol = torch.linalg.solve(ata + reg, aty)  # [n, NBASE, 2]
+        # the normal equations (one 21 x 21 system per configuration) are
+        # accumulated on the device and solved on the host: set-up, not
+        # the traced or simulated rays
+        reg = 1e-9 * torch.eye(L.SURROGATE_NBASE, dtype=torch.float64)
+        sol = torch.linalg.solve(ata.cpu() + reg, aty.cpu())  # [n, NBASE, 2]
         self.coef.copy_(sol.permute(0, 2, 1).float())
 
     # -- training ----------------------------------------------------------
@@ -365,9 +368,14 @@ class RayMapSurrogate:
         return self.history
 
     # -- inference -----------------------------------------------------------
-    def predict(self, bt, chunk: int = 131072):
+    def predict(self, bt, chunk: int = 131072, fused: bool = True):
         """Network outputs for every ray of a batch: predicted positions (mm,
-        sensor frame), logits, and the baseline positions."""
+        sensor frame), logits, and the baseline positions.  ``fused``: the
+        positions and logits come from the fused image kernel (the one that
+        simulates images), the baseline from the packing kernel; otherwise
+        everything from the layer-by-layer path."""
+        if fused:
+            return self._predict_fused(bt, chunk)
         total = bt.total
         px = torch.empty(total, device=self.dev)
         py = torch.empty(total, device=self.dev)
@@ -388,6 +396,29 @@ class RayMapSurrogate:
             by[f:f + rows] = aux[:rows, 1]
         self.mlp.check_errors()
         return {"px": px, "py": py, "logit": logit, "base_x": bx, "base_y": by}
+
+    def _predict_fused(self, bt, chunk: int):
+        total = bt.total
+        out = torch.empty((total, 4), device=self.dev)
+        base = torch.empty((total, 2), device=self.dev)
+        bufs = self.mlp.buffers(chunk, train=False)
+        for f in range(0, total, chunk):
+            rows = min(chunk, total - f)
+            self._pack(bt, f, rows, bufs)
+            base[f:f + rows] = bufs["aux"][:rows, :2]
+        stats = torch.zeros(4, dtype=torch.int64, device=self.dev)
+        net = self.mlp.desc()
+        need = int(self.lib.otx_surrogate_image_fused_workspace(ctypes.byref(bt.batch),
+                                                                ctypes.byref(net), total))
+        ws = torch.empty(max(need, 256), dtype=torch.uint8, device=self.dev)
+        st = self.lib.otx_surrogate_image_fused(
+            ctypes.byref(bt.lowering.sys), ctypes.byref(bt.batch), ctypes.byref(self.sg),
+            ctypes.byref(net), 0, total, None, ptr(out), ptr(ws), need, ptr(stats),
+            ptr(self.mlp.err), stream_handle())
+        L.check(st, "otx_surrogate_image_fused")
+        self.mlp.check_errors()
+        return {"px": out[:, 0], "py": out[:, 1], "logit": out[:, 2], "base_x": base[:, 0],
+                "base_y": base[:, 1]}
 
     def evaluate(self, bt_eval, budget_px: float = 0.05) -> dict:
         """Errors against the plain trace of a held-out batch (already run).
@@ -467,12 +498,13 @@ class RayMapSurrogate:
             net = self.mlp.desc()
             for f in range(0, total, chunk):
                 rows = min(chunk, total - f)
-                need = int(lib.otx_surrogate_image_fused_workspace(ctypes.byref(bt.batch), rows))
+                need = int(lib.otx_surrogate_image_fused_workspace(ctypes.byref(bt.batch),
+                                                                   ctypes.byref(net), rows))
                 ws = torch.empty(max(need, 256), dtype=torch.uint8, device=self.dev)
                 st = lib.otx_surrogate_image_fused(
                     ctypes.byref(bt.lowering.sys), ctypes.byref(bt.batch), ctypes.byref(self.sg),
-                    ctypes.byref(net), f, rows, ctypes.byref(bt.img), ptr(ws), need, ptr(stats),
-                    ptr(self.mlp.err), sh)
+                    ctypes.byref(net), f, rows, ctypes.byref(bt.img), None, ptr(ws), need,
+                    ptr(stats), ptr(self.mlp.err), sh)
                 L.check(st, "otx_surrogate_image_fused")
             return bt.images, stats
         chunk = chunk or 131072

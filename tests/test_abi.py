@@ -193,13 +193,13 @@ def test_fused_surrogate_validation(built_library):
         net.w[l] = 4096 * (l + 1)
         net.b[l] = 4096 * (l + 9)
         net.ld[l] = 16 if l == 0 else 256
-    need = lib.otx_surrogate_image_fused_workspace(ctypes.byref(b), 1000)
+    need = lib.otx_surrogate_image_fused_workspace(ctypes.byref(b), ctypes.byref(net), 1000)
     assert need >= 4000 and need % 256 == 0
-    assert lib.otx_surrogate_image_fused_workspace(None, 10) == -1
+    assert lib.otx_surrogate_image_fused_workspace(None, ctypes.byref(net), 10) == -1
 
     def call(count=1000, ws=256, nbytes=need, net_=net, sys_=s):
         return lib.otx_surrogate_image_fused(ctypes.byref(sys_), ctypes.byref(b), ctypes.byref(sg),
-                                             ctypes.byref(net_), 0, count, None, ws, nbytes,
+                                             ctypes.byref(net_), 0, count, None, None, ws, nbytes,
                                              256, 256, None)
 
     assert call(count=0) == L.OK  # nothing to do, no device call
