@@ -238,6 +238,17 @@ def run_surrogate(args, rank: int, world: int) -> None:
     flux_err = abs(float(sim.sum()) - float(ref.sum())) / float(ref.sum())
     l1 = float((sim.double() - ref.double()).abs().sum()) / float(ref.sum())
     surfaces = 4
+    # the network's algorithmic work per ray: 2 (9 x 256 + 3 x 256^2 + 256 x 3)
+    flops_per_ray = 2 * (9 * 256 + 3 * 256 * 256 + 256 * 3)
+    pk, pk_kind = peaks()
+    ach = flops_per_ray * total / (ms_sur * 1e-3) / 1e12
+    roofline = {
+        "bound": "tensor", "achieved": ach, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+        "frac": ach / pk["bf16_tflops"], "traffic": None, "peak_kind": pk_kind + " bf16 burst",
+        "kernel": "k_surrogate_fused (+ k_surrogate_fallback for the traced rays, one call)",
+        "kernel_ms": ms_sur, "flops_per_ray": flops_per_ray,
+        "l2_weight_bytes_per_ray": 1550,
+    }
     line = {
         "metric": "rays*surfaces/s (image simulation: MLP surrogate + traced fallback vs plain "
                   "FP32 trace)",
@@ -254,6 +265,8 @@ def run_surrogate(args, rank: int, world: int) -> None:
         "plain_trace": {"value": total * surfaces / (ms_plain * 1e-3), "ms": ms_plain},
         "surrogate_ms": ms_sur,
         "speedup_vs_plain": ms_plain / ms_sur,
+        "roofline": roofline,
+        "gpu_launches": 2,
         "held_out": {k: ev[k] for k in ("rms_px", "p999_px", "max_px", "baseline_rms_px",
                                         "baseline_p999_px", "fallback_fraction",
                                         "efficiency_rel_error", "false_pass", "false_block")},

@@ -438,7 +438,8 @@ otx_status otx_silu_backward(const float* dy, const void* z, void* dz, int64_t c
 /* out[c][r] = in[r][c] for a bf16 rows x cols matrix. */
 otx_status otx_transpose_bf16(const void* in, int32_t rows, int32_t cols, int32_t ldi, void* out,
                               int32_t ldo, void* stream);
-/* out[c] = sum over rows of in[r][c] (bf16 in, fp32 out). */
+/* out[c] = sum over rows of in[r][c] (bf16 in, fp32 out); cols <= 256, the
+ * row pitch ldi a multiple of 8 and in 16-byte aligned. */
 otx_status otx_colsum_bf16(const void* in, int32_t rows, int32_t cols, int32_t ldi, float* out,
                            void* stream);
 /* One Adam step on fp32 master weights w (rows x cols) with moments m, v;

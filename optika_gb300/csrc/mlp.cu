@@ -266,14 +266,44 @@ __global__ void k_transpose_bf16(const __nv_bfloat16* __restrict__ in, int rows,
   }
 }
 
-// out[c] = sum_r in[r][c] (bf16 in, fp32 out), one block per column chunk.
-__global__ void k_colsum_bf16(const __nv_bfloat16* __restrict__ in, int rows, int cols, int ldi,
-                              float* __restrict__ out) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= cols) return;
-  float acc = 0.f;
-  for (int r = blockIdx.y; r < rows; r += gridDim.y) acc += __bfloat162float(in[(int64_t)r * ldi + c]);
-  atomicAdd(out + c, acc);
+// out[c] += sum_r in[r][c] (bf16 in, fp32 out).  Each warp walks its own
+// rows, one row per step with a 16-byte load per lane (8 columns), so many
+// loads are in flight; the block's warps then reduce through shared memory
+// and add their column sums with one atomic per column.
+constexpr int COLSUM_BLOCK = 256;
+constexpr int COLSUM_MAX_COLS = 256;
+
+__global__ void __launch_bounds__(COLSUM_BLOCK)
+    k_colsum_bf16(const __nv_bfloat16* __restrict__ in, int rows, int cols, int ldi,
+                  float* __restrict__ out) {
+  __shared__ float part[COLSUM_BLOCK / 32][COLSUM_MAX_COLS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = gridDim.x * (COLSUM_BLOCK / 32);
+  const int c0 = lane * 8;
+  float acc[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc[i] = 0.f;
+  if (c0 < cols) {
+    for (int r = blockIdx.x * (COLSUM_BLOCK / 32) + warp; r < rows; r += nw) {
+      const uint4 q = *reinterpret_cast<const uint4*>(in + (int64_t)r * ldi + c0);
+      const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        acc[2 * i] += __uint_as_float(w[i] << 16);
+        acc[2 * i + 1] += __uint_as_float(w[i] & 0xffff0000u);
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    if (c0 + i < COLSUM_MAX_COLS) part[warp][c0 + i] = acc[i];
+  __syncthreads();
+  for (int c = threadIdx.x; c < cols; c += COLSUM_BLOCK) {
+    float t = 0.f;
+#pragma unroll
+    for (int w = 0; w < COLSUM_BLOCK / 32; ++w) t += part[w][c];
+    atomicAdd(out + c, t);
+  }
 }
 
 // Adam (Kingma and Ba, 2015) on fp32 master weights; writes the bf16
@@ -420,12 +450,17 @@ otx_status otx_transpose_bf16(const void* in, int32_t rows, int32_t cols, int32_
 otx_status otx_colsum_bf16(const void* in, int32_t rows, int32_t cols, int32_t ldi, float* out,
                            void* stream) {
   if (!in || !out || rows < 0 || cols < 0 || ldi < cols) return OTX_ERR_INVALID;
+  if (cols > COLSUM_MAX_COLS || ldi % 8 || (reinterpret_cast<uintptr_t>(in) & 15))
+    return OTX_ERR_INVALID;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   if (cudaMemsetAsync(out, 0, sizeof(float) * (size_t)cols, st) != cudaSuccess) return OTX_ERR_CUDA;
   if (rows == 0 || cols == 0) return OTX_OK;
-  dim3 grid((cols + 127) / 128, rows < 256 ? rows : 256);
-  k_colsum_bf16<<<grid, 128, 0, st>>>(reinterpret_cast<const __nv_bfloat16*>(in), rows, cols, ldi,
-                                      out);
+  const int warps = COLSUM_BLOCK / 32;
+  int grid = grid_1d((int64_t)rows, warps);  // at most 16 blocks per SM
+  const int cap = (rows + 16 * warps - 1) / (16 * warps);  // at least 16 rows per warp
+  if (grid > cap) grid = cap > 0 ? cap : 1;
+  k_colsum_bf16<<<grid, COLSUM_BLOCK, 0, st>>>(reinterpret_cast<const __nv_bfloat16*>(in), rows,
+                                               cols, ldi, out);
   return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
 }
 

@@ -135,6 +135,11 @@ def test_elementwise_training_kernels(cuda):
     cs = torch.empty(cols, device="cuda")
     assert lib.otx_colsum_bf16(ptr(z), rows, cols, cols, ptr(cs), stream_handle()) == L.OK
     assert torch.allclose(cs, zf.sum(0), atol=1e-2, rtol=1e-4)
+    # the output layer's case: 3 columns in rows of 8, many rows
+    z8 = (3 * torch.randn((70001, 8), device="cuda", generator=g)).to(torch.bfloat16)
+    cs3 = torch.empty(3, device="cuda")
+    assert lib.otx_colsum_bf16(ptr(z8), 70001, 3, 8, ptr(cs3), stream_handle()) == L.OK
+    assert torch.allclose(cs3, z8.float()[:, :3].sum(0), atol=0.1, rtol=1e-4)
 
     # three Adam steps against the closed form of Kingma and Ba (2015)
     w = torch.randn((rows, cols), device="cuda", generator=g)
