@@ -283,6 +283,224 @@ def run_surrogate(args, rank: int, world: int) -> None:
         print(json.dumps(line), flush=True)
 
 
+_BATCH_PARAMS = None
+
+
+def _cpu_batched_worker(args):
+    """One bounded chunk of the batched workload's CPU baseline: n rays of
+    configuration c through the float64 oracle, binned."""
+    c, n, seed = args
+    sys.path.insert(0, str(ROOT))
+    from optika_gb300 import configs
+    from oracle import batch as OB
+    from oracle import trace as O
+
+    global _BATCH_PARAMS
+    if _BATCH_PARAMS is None:  # the 4096 configurations the GPU traces
+        _BATCH_PARAMS = configs.spectrograph_batch(4096, seed=seed)[2]
+    s = configs.spectrograph(*_BATCH_PARAMS[c])
+    g = OB.batch_inputs(seed, c, n, *configs.SPEC_WAVELENGTH, *configs.SPEC_FIELD_HALF,
+                        configs.SPEC_PUPIL_HALF)
+    t0 = time.perf_counter()
+    r = O.rayfunction(s, *(g[k].astype(np.float64) for k in ("wavelength", "field_x", "field_y",
+                                                             "pupil_x", "pupil_y")))
+    O.collect(s.sensor, r)
+    return n, time.perf_counter() - t0
+
+
+def _cpu_pool(worker, jobs, cores):
+    import concurrent.futures
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    with concurrent.futures.ProcessPoolExecutor(max_workers=cores, mp_context=ctx) as ex:
+        list(ex.map(worker, jobs[:cores]))  # warm the workers
+        t0 = time.perf_counter()
+        res = list(ex.map(worker, jobs))
+        wall = time.perf_counter() - t0
+    return sum(r[0] for r in res), wall
+
+
+def run_batched(args, rank: int, world: int) -> None:
+    """The batched form: 4096 spectrograph configurations (spherical primary,
+    toroidal VLS grating, 2048 x 1024 sensor), log-uniform 1e3-1e6 rays each,
+    generated on the device and traced in one persistent launch with
+    per-configuration sensor images; tile and rays-per-thread from the
+    autotuner; one step replayed as a CUDA graph.  Replicas under torchrun."""
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from optika_gb300 import batch, configs
+
+    n_cfg = args.configs
+    systems, counts, _ = configs.spectrograph_batch(n_cfg, seed=3)
+    bt = batch.BatchedTrace(systems, overrides=[2, 3], ray_counts=counts, seed=3 + 1000 * rank,
+                            wavelength=configs.SPEC_WAVELENGTH,
+                            field_half=configs.SPEC_FIELD_HALF,
+                            pupil_half=configs.SPEC_PUPIL_HALF, image=True,
+                            outputs=("px", "py", "unvignetted"))
+    choice = bt.tune()
+    graph = bt.graph()
+    for _ in range(args.warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    e0.record()
+    for _ in range(args.steps):
+        graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    total = int(bt.total)
+    surfaces = 4
+    value = world * total * surfaces / (ms * 1e-3)
+    # bytes per ray: 9 B of outputs (px, py, mask) and one 4-byte image
+    # count; no input traffic (rays generated on the device)
+    bpr = 13
+    pk, pk_kind = peaks()
+    ach = bpr * total / (ms * 1e-3) / 1e9
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores = len(os.sched_getaffinity(0))
+        jobs = [(c, 50000, 3) for c in range(0, 4 * cores)]
+        n, wall = _cpu_pool(_cpu_batched_worker, jobs, cores)
+        cpu = {"value": n * surfaces / wall, "unit": "rays*surfaces/s", "cores": cores,
+               "kind": "port", "sample": f"{len(jobs)} configurations x 50000 rays ({wall:.1f} s)"}
+    if rank == 0:
+        print(json.dumps({
+            "metric": "rays*surfaces/s (batched spectrograph configurations, one persistent "
+                      "launch)",
+            "value": value, "unit": "rays*surfaces/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Philox rays on the device)",
+            "config": {"workload": "spectrograph-batched", "configs": n_cfg, "rays": total,
+                       "surfaces": surfaces, "sensor": "2048x1024 x 13.5um per configuration",
+                       "schedule": {"tile": choice[0], "rays_per_thread": choice[1]},
+                       "cuda_graph": True},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": ach / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+                         "bytes_per_ray": bpr, "kernel": "k_trace_batch (spectrograph shape)",
+                         "kernel_ms": ms,
+                         "note": "compute-bound (FP32 issue): the byte roofline is shown for "
+                                 "completeness"},
+            "cpu_baseline": cpu, "gpu_launches": 3, "clocks": clk,
+        }), flush=True)
+
+
+def _cpu_multilayer_worker(args):
+    c, n, seed = args
+    sys.path.insert(0, str(ROOT))
+    from oracle import trace as O
+
+    mirrors = _mirrors(seed, c + 1)
+    rng = np.random.default_rng(1000 + c)
+    wl = rng.uniform(12.0, 15.0, n)
+    cos = np.cos(rng.uniform(0.0, 20.0 * math.pi / 180.0, n))
+    m = mirrors[c]
+    t0 = time.perf_counter()
+    O.multilayer_efficiency(wl, cos, 1.0, m.layers, m.substrate)
+    return n, time.perf_counter() - t0
+
+
+def _mirrors(seed: int, count: int):
+    """Periodic bilayer mirrors of the multilayer workload: period U(9.5,
+    10.5) nm, thickness ratio 0.4, indices 1 - delta + i beta with delta
+    log-uniform in [1e-3, 1e-1] and beta in [1e-4, 1e-2]."""
+    import optika_gb300 as ok
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        d = rng.uniform(9.5, 10.5)
+
+        def idx():
+            delta = 10 ** rng.uniform(-3, -1)
+            beta = 10 ** rng.uniform(-4, -2)
+            z = 1 - delta + 1j * beta
+            return complex(np.float32(z.real), np.float32(z.imag))
+
+        out.append(ok.materials.PeriodicMirror(
+            a=ok.materials.Layer(idx(), float(np.float32(0.4 * d))),
+            b=ok.materials.Layer(idx(), float(np.float32(0.6 * d))),
+            num_periods=40, substrate=ok.materials.Layer(idx())))
+    return out
+
+
+def run_multilayer(args, rank: int, world: int) -> None:
+    """The multilayer form: 256 periodic 40-bilayer mirrors, 1e7 samples
+    (wavelength U(12, 15) nm, incidence U(0, 20) deg, a mirror each), R and
+    T for s and p from float-float transfer matrices.  Inputs resident in
+    HBM.  Replicas under torchrun."""
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from optika_gb300 import _api
+    from optika_gb300 import _lib as L
+
+    n = args.samples
+    mirrors = _mirrors(4, 256)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g = torch.Generator(device=dev).manual_seed(4 + 1000 * rank)
+    wl = 12.0 + 3.0 * torch.rand(n, device=dev, generator=g)
+    cos = torch.cos(torch.rand(n, device=dev, generator=g) * (20.0 * math.pi / 180.0))
+    index = torch.randint(0, 256, (n,), device=dev, generator=g, dtype=torch.int32)
+    table = _api.periodic_table(mirrors, dev)
+    outs = [torch.empty(n, device=dev) for _ in range(4)]
+    lib = L.load()
+
+    def step():
+        st = lib.otx_multilayer_periodic(
+            _api.ptr(table), len(mirrors), n, _api.ptr(wl), 1, _api.ptr(cos), 1,
+            _api.ptr(index), 1.0, 0.0, *(_api.ptr(o) for o in outs), _api.stream_handle())
+        L.check(st, "otx_multilayer_periodic")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    value = world * n / (ms * 1e-3)
+    bps = 12 + 16  # wavelength, cosine, mirror index in; R_s, R_p, T_s, T_p out
+    pk, pk_kind = peaks()
+    ach = bps * n / (ms * 1e-3) / 1e9
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores = len(os.sched_getaffinity(0))
+        jobs = [(c, 30000, 4) for c in range(0, 4 * cores)]
+        m, wall = _cpu_pool(_cpu_multilayer_worker, jobs, cores)
+        cpu = {"value": m / wall, "unit": "samples/s (s and p)", "cores": cores, "kind": "port",
+               "sample": f"{len(jobs)} mirrors x 30000 samples, complex128 ({wall:.1f} s)"}
+    if rank == 0:
+        print(json.dumps({
+            "metric": "multilayer samples/s (R and T, s and p, 40-bilayer periodic mirrors)",
+            "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float-float products)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "multilayer-periodic", "mirrors": 256, "samples": n,
+                       "bilayers": 40, "l2": "inputs and outputs 280 MB, larger than L2"},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": ach / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+                         "bytes_per_sample": bps, "kernel": "k_multilayer_periodic",
+                         "kernel_ms": ms,
+                         "note": "compute-bound (FP32 issue): the byte roofline is shown for "
+                                 "completeness"},
+            "cpu_baseline": cpu, "gpu_launches": args.steps, "clocks": clk,
+        }), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -295,7 +513,11 @@ def main() -> None:
     ap.add_argument("--ref-rays", type=int, default=2_000_000,
                     help="rays per step of the reference (CPU) arm")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="precision", choices=["precision", "surrogate"])
+    ap.add_argument("--workload", default="precision",
+                    choices=["precision", "surrogate", "batched", "multilayer"])
+    ap.add_argument("--configs", type=int, default=4096, help="batched workload configurations")
+    ap.add_argument("--samples", type=int, default=10_000_000,
+                    help="multilayer workload samples per step")
     ap.add_argument("--train-steps", type=int, default=6000)
     ap.add_argument("--image-rays", type=int, default=1_000_000_000)
     ap.add_argument("--image-chunk", type=int, default=0,
@@ -314,6 +536,12 @@ def main() -> None:
         return
     if args.workload == "surrogate":
         run_surrogate(args, rank, world)
+        return
+    if args.workload == "batched":
+        run_batched(args, rank, world)
+        return
+    if args.workload == "multilayer":
+        run_multilayer(args, rank, world)
         return
 
     import torch

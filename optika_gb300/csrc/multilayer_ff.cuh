@@ -264,4 +264,158 @@ __device__ __forceinline__ void multilayer_pol_ff(const S& src, float wl, float 
   }
 }
 
+// ---------------------------------------------------------------- bilayer mirrors
+
+// The propagation factors exp(-i beta), exp(+i beta) of one layer, beta =
+// 2 pi h (n cos) / lambda, and whether the layer is transparent enough to
+// enter the product (|exp(-i beta)| < 1e10).  n cos is the same for s and
+// p (the p-medium factor conj(q_p) |n|^2 equals q_s), so one evaluation
+// serves both polarisations and every period.
+struct LayerPhase {
+  cff em, ep;
+  bool prop;
+};
+
+__device__ __forceinline__ LayerPhase layer_phase_ff(const cff& w, float thickness, float wl) {
+  const ff k = ff_div(ff_mulf(ff_2pi(), thickness), ff_of(wl));
+  const cff beta = cff_scale(w, k);
+  ff sn, cs;
+  ff_sincos(beta.re, sn, cs);
+  const ff g = ff_exp(beta.im);
+  LayerPhase L;
+  L.prop = g.hi < 1e10f;
+  L.em = cff{ff_mul(g, cs), ff_neg(ff_mul(g, sn))};
+  const ff gi = ff_div(ff_of(1.f), g);
+  L.ep = cff{ff_mul(gi, cs), ff_mul(gi, sn)};
+  return L;
+}
+
+// One interface (and layer) step of the product, as layer_step_ff: the
+// matrix from the current medium q into qj, with the layer's propagation
+// when ph is given.
+__device__ __forceinline__ void bilayer_step(MLff& st, const cff& qj, const LayerPhase* ph) {
+  const cff a = cff_add(st.q, qj), b = cff_sub(st.q, qj);
+  cmff tm{a, b, b, a};
+  bool wprop = true;
+  if (ph) {
+    wprop = ph->prop;
+    if (wprop) tm = cmff{cff_mul(a, ph->em), cff_mul(b, ph->ep), cff_mul(b, ph->em), cff_mul(a, ph->ep)};
+  }
+  if (st.where) {
+    mlff_times(st, tm, 0);
+    st.t = ff_mul(st.t, ff_scale2(cff_abs2(st.q), 4.f));
+    ff_normalize_scalar(st.t, st.te);
+  }
+  st.where = st.where && wprop;
+  st.q = qj;
+}
+
+// t^e (e >= 1) for a normalised positive scalar, exponent tracked in te.
+__device__ __forceinline__ void ff_pow_scalar(ff t, int te, int e, ff& out, int& oute) {
+  bool first = true;
+  while (e > 0) {
+    if (e & 1) {
+      if (first) {
+        out = t;
+        oute = te;
+        first = false;
+      } else {
+        out = ff_mul(out, t);
+        oute += te;
+        ff_normalize_scalar(out, oute);
+      }
+    }
+    e >>= 1;
+    if (e) {
+      t = ff_mul(t, t);
+      te *= 2;
+      ff_normalize_scalar(t, te);
+    }
+  }
+}
+
+// R and T of one polarisation of [A, B] x periods on a substrate, given the
+// media factors q0 (ambient), qa, qb, qs and the two layers' phases: the
+// steps and the period power of multilayer_pol_ff for a periodic stack,
+// with the transmission factor of the repeated periods raised by squaring.
+__device__ __forceinline__ void bilayer_pol_ff(const cff& q0, const cff& qa, const cff& qb,
+                                               const cff& qs, const LayerPhase& A,
+                                               const LayerPhase& B, int periods, float& R,
+                                               float& T) {
+  MLff st;
+  st.e = 0;
+  st.first = true;
+  st.t = ff_of(1.f);
+  st.te = 0;
+  st.q = q0;
+  st.where = true;
+  if (periods > 0) {
+    bilayer_step(st, qa, &A);  // first period
+    bilayer_step(st, qb, &B);
+    MLff per = st;
+    per.first = true;
+    per.e = 0;
+    per.t = ff_of(1.f);
+    per.te = 0;
+    bilayer_step(per, qa, &A);  // the period, from its own last medium
+    bilayer_step(per, qb, &B);
+    const int reps = periods - 1;
+    if (!per.first && reps > 0) {
+      cmff pm;
+      int pe = 0;
+      cmff_pow(per.m, per.e, reps, pm, pe);
+      mlff_times(st, pm, pe);
+      ff pt;
+      int pte = 0;
+      ff_pow_scalar(per.t, per.te, reps, pt, pte);
+      st.t = ff_mul(st.t, pt);
+      st.te += pte;
+      ff_normalize_scalar(st.t, st.te);
+    }
+    st.where = per.where;
+    st.q = per.q;
+  }
+  bilayer_step(st, qs, nullptr);  // into the substrate
+  const ff m11 = cff_abs2(st.m.a);
+  R = ff_to_f(ff_div(cff_abs2(st.m.c), m11));
+  T = 0.f;
+  if (st.where) {
+    const ff ratio = cff_div(st.q, q0).re;
+    const ff tt = ff_mul(ff_div(st.t, m11), ratio);
+    T = ldexpf(ff_to_f(tt), st.te - 2 * st.e);
+  }
+}
+
+// Medium factor n cos of the medium of index nj for the ambient's
+// invariant inv0 = (n0 sin0)^2 (the s factor q_s).
+__device__ __forceinline__ cff medium_w_ff(const cff& inv0, cf nj_f) {
+  const cff nj = cff_of(nj_f.re, nj_f.im);
+  const cff cj = cff_sqrt(cff_sub(cff_of(1.f, 0.f), cff_div(inv0, cff_mul(nj, nj))));
+  return cff_mul(nj, cj);
+}
+
+// p factor conj(q_s) / |n|^2 from the s factor.
+__device__ __forceinline__ cff p_factor(const cff& w, cf nj_f) {
+  return cff_scale(cff_conj(w), ff_div(ff_of(1.f), cff_abs2(cff_of(nj_f.re, nj_f.im))));
+}
+
+// R and T, s and p, of a periodic bilayer mirror (float-float): the layer
+// phases are evaluated once per sample.
+__device__ __forceinline__ void periodic_bilayer_ff(const otx_periodic_stack& P, float wl,
+                                                    float cos0, cf n0, float& Rs, float& Rp,
+                                                    float& Ts, float& Tp) {
+  const cff n0c = cff_of(n0.re, n0.im);
+  const ff one_m_c2 = ff_sub(ff_of(1.f), ff_mul(ff_of(cos0), ff_of(cos0)));
+  const cff inv0 = cff_scale(cff_mul(n0c, n0c), one_m_c2);
+  const cf na{P.n_a_re, P.n_a_im}, nb{P.n_b_re, P.n_b_im}, ns{P.n_sub_re, P.n_sub_im};
+  const cff wa = medium_w_ff(inv0, na), wb = medium_w_ff(inv0, nb), ws = medium_w_ff(inv0, ns);
+  const LayerPhase A = layer_phase_ff(wa, P.thickness_a, wl);
+  const LayerPhase B = layer_phase_ff(wb, P.thickness_b, wl);
+  const cff q0s = cff_scale(n0c, ff_of(cos0));
+  bilayer_pol_ff(q0s, wa, wb, ws, A, B, P.num_periods, Rs, Ts);
+  const cff q0p = cff_scale(cff_conj(n0c), ff_div(ff_of(cos0), cff_abs2(n0c)));
+  bilayer_pol_ff(q0p, p_factor(wa, na), p_factor(wb, nb), p_factor(ws, ns), A, B,
+                 P.num_periods, Rp, Tp);
+}
+
 }  // namespace otx
