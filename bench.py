@@ -365,10 +365,10 @@ def run_batched(args, rank: int, world: int) -> None:
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
-        jobs = [(c, 50000, 3) for c in range(0, 4 * cores)]
+        jobs = [(c, 400000, 3) for c in range(0, 4 * cores)]
         n, wall = _cpu_pool(_cpu_batched_worker, jobs, cores)
         cpu = {"value": n * surfaces / wall, "unit": "rays*surfaces/s", "cores": cores,
-               "kind": "port", "sample": f"{len(jobs)} configurations x 50000 rays ({wall:.1f} s)"}
+               "kind": "port", "sample": f"{len(jobs)} configurations x 400000 rays ({wall:.1f} s)"}
     if rank == 0:
         print(json.dumps({
             "metric": "rays*surfaces/s (batched spectrograph configurations, one persistent "

@@ -194,3 +194,67 @@ def spectrograph_batch(num_configs: int = 4096, seed: int = 3, min_rays: int = 1
     params = np.stack([d0, a1, a2, tilt], axis=-1)
     systems_ = [spectrograph(*p) for p in params]
     return systems_, counts.astype(np.int64), params
+
+
+# -------------------------------------------------- systems with stops
+# The two stop-solver systems of the reference's tests
+# (optika/systems/_sequential_test.py:536-575 and 599-646), in mm and rad.
+
+STOP_NEWTONIAN_FIELD = 0.05 * DEG
+STOP_GRAZING_FIELD = 0.25 * DEG
+
+
+def stop_newtonian() -> systems.SequentialSystem:
+    """Spherical primary (R -2000 mm, r 50 mm) at z = 500 mm, the pupil stop
+    (r 10 mm) downstream at z = 250 mm, the sensor (128^2 x 15 um) at
+    z = -500 mm; the object is the field stop, an angular aperture of
+    radius sin(0.05 deg)."""
+    obj = surfaces.Surface(
+        name="source",
+        aperture=apertures.CircularAperture(math.sin(STOP_NEWTONIAN_FIELD), dimensionless=True),
+        is_field_stop=True,
+    )
+    primary = surfaces.Surface(
+        name="primary", sag=sags.SphericalSag(-2000.0), material=materials.Mirror(),
+        aperture=apertures.CircularAperture(50.0),
+        transformation=transforms.Translation(z=500.0),
+    )
+    stop = surfaces.Surface(
+        name="aperture", aperture=apertures.CircularAperture(10.0), is_pupil_stop=True,
+        transformation=transforms.Translation(z=250.0),
+    )
+    sensor = sensors.ImagingSensor(
+        name="sensor", width_pixel=0.015, num_pixel=(128, 128),
+        transformation=transforms.Translation(z=-500.0),
+    )
+    return systems.SequentialSystem(object=obj, surfaces=[primary, stop], sensor=sensor)
+
+
+def stop_grazing() -> systems.SequentialSystem:
+    """Parabolic primary (f -2000 mm, r 260 mm, the pupil stop) at
+    z = 2500 mm, a transmission grating (10 um spacing, order +1, 60 mm
+    square) at z = 1000 mm, the sensor (2048 x 1024 x 15 um) at x = 26,
+    z = 480 mm; the object is the field stop, an angular aperture of radius
+    sin(0.25 deg)."""
+    from . import rulings
+
+    obj = surfaces.Surface(
+        name="source",
+        aperture=apertures.CircularAperture(math.sin(STOP_GRAZING_FIELD), dimensionless=True),
+        is_field_stop=True,
+    )
+    primary = surfaces.Surface(
+        name="paraboloid", sag=sags.ParabolicSag(focal_length=-2000.0),
+        material=materials.Mirror(), aperture=apertures.CircularAperture(260.0),
+        is_pupil_stop=True, transformation=transforms.Translation(z=2500.0),
+    )
+    grating = surfaces.Surface(
+        name="grating", rulings=rulings.Rulings(spacing=0.010, diffraction_order=1),
+        aperture=apertures.RectangularAperture(half_width=60.0),
+        transformation=transforms.Translation(z=1000.0),
+    )
+    sensor = sensors.ImagingSensor(
+        name="sensor", width_pixel=0.015, num_pixel=(2048, 1024),
+        transformation=transforms.Translation(x=26.0, z=480.0),
+    )
+    return systems.SequentialSystem(object=obj, surfaces=[primary, grating], sensor=sensor)

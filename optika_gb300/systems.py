@@ -3,15 +3,18 @@
 :meth:`SequentialSystem.raytrace` and :meth:`SequentialSystem.rayfunction`
 build the input rays from a (wavelength, field, pupil) grid and trace them
 through ``[object] + surfaces + [sensor]`` in one fused GPU launch
-(optika/systems/_sequential.py:791-988).  Field and pupil coordinates must
-be physical (``normalized_field=False, normalized_pupil=False``): the stop
-solve behind normalised coordinates (:396-789) is not part of this build.
+(optika/systems/_sequential.py:791-988).  Normalised field and pupil
+coordinates (the default, as in the reference) are mapped to physical ones
+through the extents of the field and pupil stops, which the stop solver
+(:mod:`optika_gb300.stops`) finds on the GPU (:396-850).
 """
 
 from __future__ import annotations
 
 import dataclasses
 from typing import Sequence
+
+import numpy as np
 
 from . import _lib as L
 from . import transforms
@@ -49,19 +52,88 @@ class SequentialSystem:
             out.append(self.sensor)
         return out
 
-    def _grid(self, wavelength, field, pupil, normalized_field, normalized_pupil):
-        if normalized_field or normalized_pupil:
-            raise NotImplementedError(
-                "normalized field/pupil coordinates need the stop solver, which this build "
-                "does not provide; pass physical coordinates with "
-                "normalized_field=False, normalized_pupil=False"
-            )
+    # ---- stops (optika/systems/_sequential.py:262-341, 755-799)
+
+    @property
+    def index_field_stop(self) -> int:
+        idx = [i for i, s in enumerate(self.surfaces_all) if s.is_field_stop]
+        if not idx:
+            raise ValueError("field stop is not defined for this system; set "
+                             "`is_field_stop=True` for at least one surface")
+        return idx[-1]
+
+    @property
+    def index_pupil_stop(self) -> int:
+        idx = [i for i, s in enumerate(self.surfaces_all) if s.is_pupil_stop]
+        if not idx:
+            raise ValueError("pupil stop is not defined for this system; set "
+                             "`is_pupil_stop=True` for at least one surface")
+        return idx[-1]
+
+    @property
+    def field_stop(self) -> AbstractSurface:
+        return self.surfaces_all[self.index_field_stop]
+
+    @property
+    def pupil_stop(self) -> AbstractSurface:
+        return self.surfaces_all[self.index_pupil_stop]
+
+    def _wavelength_input(self) -> float:
         g = self.grid_input if self.grid_input is not None else ObjectVectorArray()
-        return (
-            g.wavelength if wavelength is None else wavelength,
-            g.field if field is None else field,
-            g.pupil if pupil is None else pupil,
-        )
+        w = np.unique(np.asarray(g.wavelength, dtype=np.float64))
+        if len(w) != 1:
+            raise ValueError("field_min/max and pupil_min/max need a single input wavelength")
+        return float(w[0])
+
+    def rayfunction_stops(self, wavelength: None | float = None) -> dict:
+        """Rays from the object that strike the edges of both stops, with
+        the field and pupil grids they give (torch tensors [first stop
+        wire, last stop wire], 21 x 21)."""
+        from .stops import rayfunction_stops
+
+        w = self._wavelength_input() if wavelength is None else float(wavelength)
+        return rayfunction_stops(self, w)
+
+    @property
+    def field_min(self) -> tuple[float, float]:
+        """Lower corner of the field of view (rad at infinity, else mm)."""
+        from .stops import extents
+
+        return extents(self, self._wavelength_input())[0]
+
+    @property
+    def field_max(self) -> tuple[float, float]:
+        from .stops import extents
+
+        return extents(self, self._wavelength_input())[1]
+
+    @property
+    def pupil_min(self) -> tuple[float, float]:
+        """Lower corner of the entrance pupil (mm at infinity, else rad)."""
+        from .stops import extents
+
+        return extents(self, self._wavelength_input())[2]
+
+    @property
+    def pupil_max(self) -> tuple[float, float]:
+        from .stops import extents
+
+        return extents(self, self._wavelength_input())[3]
+
+    def _grid(self, wavelength, field, pupil, normalized_field, normalized_pupil):
+        g = self.grid_input if self.grid_input is not None else ObjectVectorArray()
+        wl = g.wavelength if wavelength is None else wavelength
+        fld = g.field if field is None else field
+        pup = g.pupil if pupil is None else pupil
+        if normalized_field or normalized_pupil:
+            from .stops import denormalize
+            from .vectors import Cartesian2dVectorArray
+
+            (fx, fy), (qx, qy) = denormalize(self, wl, (fld.x, fld.y), (pup.x, pup.y),
+                                             normalized_field, normalized_pupil)
+            fld = Cartesian2dVectorArray(fx, fy)
+            pup = Cartesian2dVectorArray(qx, qy)
+        return wl, fld, pup
 
     def raytrace(
         self,

@@ -95,9 +95,11 @@ def test_polynomial_power_limit():
                        input_mode=L.INPUT_RAYS)
 
 
-def test_normalized_coordinates_need_stop_solver():
+def test_normalized_coordinates_need_stops():
+    """Normalised coordinates (the default) need a field and a pupil stop;
+    without them the stop solver refuses before any device work."""
     s = configs.newtonian()
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(ValueError, match="not defined"):
         s.raytrace()
 
 
