@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define OTX_ABI_VERSION 1
+#define OTX_ABI_VERSION 2
 
 #define OTX_MAX_SURFACES 16
 #define OTX_MAX_POLY_TERMS 8
@@ -222,9 +222,16 @@ typedef struct otx_grid {
   int64_t count;
 } otx_grid;
 
+/* Sensor images, each [num_w][num_x][num_y] or 0 (not produced):
+ * counts: uint32 ray counts; flux: float sum of intensity (the reference's
+ * image, optika/sensors/_sensors.py:155); cos_moment: float sum of intensity
+ * times the cosine of incidence on the sensor, -direction . normal (the
+ * refracted cosine of an ideal sensor material, :156-169 and
+ * optika/sensors/materials/_materials.py:1603-1616). */
 typedef struct otx_image {
-  uint64_t counts; /* uint32_t[num_w][num_x][num_y] or 0 */
-  uint64_t flux;   /* float   [num_w][num_x][num_y] or 0 */
+  uint64_t counts;
+  uint64_t flux;
+  uint64_t cos_moment;
 } otx_image;
 
 /* Batched trace of many configurations of one system shape.  Each config

@@ -110,7 +110,7 @@ def _to_ray_array(b: dict, shape: tuple) -> RayVectorArray:
     )
 
 
-def _image_buffers(sensor, wavelength_bins, dev):
+def _image_buffers(sensor, wavelength_bins, dev, cos_moment: bool = False):
     nx, ny = sensor.num_pixel
     nw = 1 if wavelength_bins is None else int(wavelength_bins[2])
     counts = torch.zeros((nw, int(nx), int(ny)), dtype=torch.int32, device=dev)
@@ -118,6 +118,10 @@ def _image_buffers(sensor, wavelength_bins, dev):
     img = L.Image()
     img.counts = counts.data_ptr()
     img.flux = flux.data_ptr()
+    if cos_moment:
+        mom = torch.zeros((nw, int(nx), int(ny)), dtype=torch.float32, device=dev)
+        img.cos_moment = mom.data_ptr()
+        return counts, flux, img, mom
     return counts, flux, img
 
 
@@ -401,8 +405,10 @@ def propagate_rays(surfaces: Sequence, rays: RayVectorArray, accumulate: bool = 
     return _to_ray_array(bufs, shape)
 
 
-def collect(sensor, rays: RayVectorArray, wavelength=None, where=True):
-    """optika/sensors/_sensors.py:92-161 on the GPU: (counts, flux) images."""
+def collect(sensor, rays: RayVectorArray, wavelength=None, where=True, cos_moment=False):
+    """optika/sensors/_sensors.py:92-169 on the GPU: (counts, flux) images,
+    and with ``cos_moment`` the flux-weighted sum of the cosine of
+    incidence as a third image."""
     dev = device()
     b_in, shape, n = _rays_inputs(rays, dev)
     if where is not True:
@@ -411,12 +417,15 @@ def collect(sensor, rays: RayVectorArray, wavelength=None, where=True):
         b_in["unvignetted"] = (b_in["unvignetted"].bool() & w.bool()).to(torch.uint8)
     lw = lower_surfaces([sensor], pre=np.eye(4), final=None, input_mode=L.INPUT_RAYS,
                         sensor=sensor, wavelength_bins=wavelength)
-    counts, flux, img = _image_buffers(sensor, wavelength, dev)
+    bufs = _image_buffers(sensor, wavelength, dev, cos_moment=cos_moment)
+    img = bufs[2]
     lib = L.load()
     st = lib.otx_collect(ctypes.byref(lw.sys.sensor), ctypes.byref(_rays_struct(b_in, n)),
                          ctypes.byref(img), stream_handle())
     L.check(st, "otx_collect")
-    return counts, flux
+    if cos_moment:
+        return bufs[0], bufs[1], bufs[3]
+    return bufs[0], bufs[1]
 
 
 def _sag_system(sag) -> L.System:

@@ -10,7 +10,7 @@ from __future__ import annotations
 import ctypes
 import pathlib
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_SURFACES = 16
 MAX_POLY_TERMS = 8
 MAX_VERTICES = 64
@@ -205,7 +205,7 @@ class Grid(ctypes.Structure):
 
 
 class Image(ctypes.Structure):
-    _fields_ = [("counts", u64), ("flux", u64)]
+    _fields_ = [("counts", u64), ("flux", u64), ("cos_moment", u64)]
 
 
 class Batch(ctypes.Structure):

@@ -27,8 +27,9 @@ __device__ __forceinline__ int64_t collect_bin(const otx_sensor& S, float x, flo
   return ((int64_t)iw * S.num_x + ix) * S.num_y + iy;
 }
 
-// optika/sensors/_sensors.py:92-161: histogram of position.xy (and
-// wavelength) weighted by intensity * unvignetted.
+// optika/sensors/_sensors.py:92-169: histogram of position.xy (and
+// wavelength) weighted by intensity * unvignetted, and of the same weight
+// times the cosine of incidence dz (flat sensor, normal -z).
 __global__ void k_collect(const otx_sensor S, const otx_rays r, const otx_image img) {
   const int64_t step = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < r.count; i += step) {
@@ -39,9 +40,11 @@ __global__ void k_collect(const otx_sensor S, const otx_rays r, const otx_image 
     const int64_t b = collect_bin(S, x, y, wl);
     if (b < 0) continue;
     if (img.counts) atomicAdd(reinterpret_cast<unsigned int*>(img.counts) + b, 1u);
-    if (img.flux) {
-      const float w = r.intensity ? reinterpret_cast<const float*>(r.intensity)[i] : 1.f;
-      atomicAdd(reinterpret_cast<float*>(img.flux) + b, w);
+    const float w = r.intensity ? reinterpret_cast<const float*>(r.intensity)[i] : 1.f;
+    if (img.flux) atomicAdd(reinterpret_cast<float*>(img.flux) + b, w);
+    if (img.cos_moment) {
+      const float dz = r.dz ? reinterpret_cast<const float*>(r.dz)[i] : 1.f;
+      atomicAdd(reinterpret_cast<float*>(img.cos_moment) + b, w * dz);
     }
   }
 }

@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const __grid_constant__ otx
   const int64_t* offs = reinterpret_cast<const int64_t*>(b.ray_offset);
   const int32_t* tiles = reinterpret_cast<const int32_t*>(b.tiles);
   unsigned int* counter = reinterpret_cast<unsigned int*>(b.counter);
-  const bool bin = (a.img.counts != 0) || (a.img.flux != 0);
+  const bool bin = image_any(a.img);
   int cur = -1;
   for (;;) {
     __syncthreads();  // previous item done: s_item and surf may be rewritten
@@ -86,6 +86,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const __grid_constant__ otx
             const int64_t off = (int64_t)cfg * b.image_stride;
             if (img.counts) img.counts += off * 4;
             if (img.flux) img.flux += off * 4;
+            if (img.cos_moment) img.cos_moment += off * 4;
             bin_ray(sys.sensor, img, r[k]);
           }
           store_ray<true>(a.out, base + i, sys.final_to_output, r[k]);

@@ -409,13 +409,34 @@ __device__ __forceinline__ void periodic_bilayer_ff(const otx_periodic_stack& P,
   const cff inv0 = cff_scale(cff_mul(n0c, n0c), one_m_c2);
   const cf na{P.n_a_re, P.n_a_im}, nb{P.n_b_re, P.n_b_im}, ns{P.n_sub_re, P.n_sub_im};
   const cff wa = medium_w_ff(inv0, na), wb = medium_w_ff(inv0, nb), ws = medium_w_ff(inv0, ns);
-  const LayerPhase A = layer_phase_ff(wa, P.thickness_a, wl);
-  const LayerPhase B = layer_phase_ff(wb, P.thickness_b, wl);
-  const cff q0s = cff_scale(n0c, ff_of(cos0));
-  bilayer_pol_ff(q0s, wa, wb, ws, A, B, P.num_periods, Rs, Ts);
-  const cff q0p = cff_scale(cff_conj(n0c), ff_div(ff_of(cos0), cff_abs2(n0c)));
-  bilayer_pol_ff(q0p, p_factor(wa, na), p_factor(wb, nb), p_factor(ws, ns), A, B,
-                 P.num_periods, Rp, Tp);
+  LayerPhase ph[2];
+#pragma unroll 1
+  for (int j = 0; j < 2; ++j)
+    ph[j] = layer_phase_ff(j == 0 ? wa : wb, j == 0 ? P.thickness_a : P.thickness_b, wl);
+  const LayerPhase A = ph[0], B = ph[1];
+  // one rolled loop over the polarisations keeps a single copy of the
+  // (large) float-float product code in the instruction cache
+  float R[2], T[2];
+#pragma unroll 1
+  for (int pol = 0; pol < 2; ++pol) {
+    cff q0, qa, qb, qs;
+    if (pol == 0) {
+      q0 = cff_scale(n0c, ff_of(cos0));
+      qa = wa;
+      qb = wb;
+      qs = ws;
+    } else {
+      q0 = cff_scale(cff_conj(n0c), ff_div(ff_of(cos0), cff_abs2(n0c)));
+      qa = p_factor(wa, na);
+      qb = p_factor(wb, nb);
+      qs = p_factor(ws, ns);
+    }
+    bilayer_pol_ff(q0, qa, qb, qs, A, B, P.num_periods, R[pol], T[pol]);
+  }
+  Rs = R[0];
+  Ts = T[0];
+  Rp = R[1];
+  Tp = T[1];
 }
 
 }  // namespace otx

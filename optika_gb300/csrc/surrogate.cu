@@ -322,6 +322,8 @@ otx_status otx_surrogate_image(const otx_system* base, const otx_batch* batch,
     if (b.override_index[j] < 0 || b.override_index[j] >= base->num_surfaces)
       return OTX_ERR_INVALID;
   if (b.num_overrides > 0 && !b.overrides) return OTX_ERR_INVALID;
+  // the network predicts no direction: no cosine moment from this path
+  if (image && image->cos_moment) return OTX_ERR_UNSUPPORTED;
   const bool bin = image && (image->counts || image->flux);
   if (bin && (base->sensor.num_x < 1 || base->sensor.num_y < 1 || base->sensor.num_w < 1 ||
               !(base->sensor.width_x > 0.f) || !(base->sensor.width_y > 0.f) ||

@@ -61,6 +61,7 @@ __device__ __forceinline__ otx_image config_image(const otx_image& img, int64_t 
   const int64_t off = (int64_t)cfg * stride * 4;
   if (o.counts) o.counts += off;
   if (o.flux) o.flux += off;
+  if (o.cos_moment) o.cos_moment += off;
   return o;
 }
 

@@ -504,6 +504,8 @@ otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* ba
     const int in = l == 0 ? net->num_inputs : F_WIDTH;
     if (net->ld[l] < in) return OTX_ERR_INVALID;
   }
+  // the network predicts no direction: no cosine moment from this path
+  if (image && image->cos_moment) return OTX_ERR_UNSUPPORTED;
   const bool bin = image && (image->counts || image->flux);
   if (bin && (base->sensor.num_x < 1 || base->sensor.num_y < 1 || base->sensor.num_w < 1 ||
               !(base->sensor.width_x > 0.f) || !(base->sensor.width_y > 0.f) ||

@@ -68,7 +68,7 @@ static otx_status validate_system(const otx_system* sys) {
 }
 
 static otx_status validate_image(const otx_system* sys, const otx_image* img) {
-  if (!img || (!img->counts && !img->flux)) return OTX_OK;
+  if (!img || !image_any(*img)) return OTX_OK;
   const otx_sensor& S = sys->sensor;
   if (S.num_x < 1 || S.num_y < 1 || S.num_w < 1) return OTX_ERR_INVALID;
   if (!(S.width_x > 0.f) || !(S.width_y > 0.f)) return OTX_ERR_INVALID;

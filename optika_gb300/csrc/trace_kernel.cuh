@@ -122,6 +122,8 @@ __device__ __forceinline__ void bin_ray(const otx_sensor& S, const otx_image& im
   if (b < 0) return;
   if (img.counts) atomicAdd(reinterpret_cast<unsigned int*>(img.counts) + b, 1u);
   if (img.flux) atomicAdd(reinterpret_cast<float*>(img.flux) + b, r.inten);
+  // cosine of incidence on the flat sensor (normal -z in its frame): dz
+  if (img.cos_moment) atomicAdd(reinterpret_cast<float*>(img.cos_moment) + b, r.inten * r.dz);
 }
 
 // Minimum resident CTAs per SM requested from the register allocator
@@ -137,7 +139,7 @@ __global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
   const int64_t n = a.count;
   const int64_t step = (int64_t)gridDim.x * blockDim.x * RPT;
   const int ns = sys.num_surfaces;
-  const bool bin = (a.img.counts != 0) || (a.img.flux != 0);
+  const bool bin = image_any(a.img);
   const bool final_identity = (sys.flags & OTX_SYS_FLAG_FINAL_IDENTITY) != 0;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x * RPT + threadIdx.x; base < n;
        base += step) {
@@ -191,7 +193,7 @@ __global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
                   const __grid_constant__ TraceArgs a) {
   const int64_t n = a.count;
   const int64_t step = (int64_t)gridDim.x * blockDim.x;
-  const bool bin = (a.img.counts != 0) || (a.img.flux != 0);
+  const bool bin = image_any(a.img);
   const bool final_identity = (sys.flags & OTX_SYS_FLAG_FINAL_IDENTITY) != 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
     Ray r;

@@ -9,6 +9,11 @@
 
 namespace otx {
 
+// Whether any sensor image of the call is produced.
+__host__ __device__ __forceinline__ bool image_any(const otx_image& img) {
+  return img.counts != 0 || img.flux != 0 || img.cos_moment != 0;
+}
+
 struct TraceArgs {
   otx_rays in;
   otx_grid grid;

@@ -69,11 +69,25 @@ class ImagingSensor(AbstractSurface):
         return _apertures.RectangularAperture(half_width=(wx * nx / 2, wy * ny / 2))
 
     def collect(self, rays, wavelength=None, where=True):
-        """Bin rays (in this sensor's local frame) into ``(counts, flux)``.
+        """Bin rays (in this sensor's local frame) onto the pixel grid:
+        ``(image, direction)``, the intensity image and the flux-weighted
+        mean cosine of incidence in each pixel (1 where a pixel is empty),
+        as optika/sensors/_sensors.py:92-169 returns them for an ideal
+        sensor material.  Images are ``[num_w, num_x, num_y]``.
 
         ``wavelength`` is ``None`` (one bin, all wavelengths) or
         ``(start, stop, num)`` uniform wavelength edges in nm.
         """
+        import torch
+
+        from ._api import collect
+
+        _, flux, mom = collect(self, rays, wavelength=wavelength, where=where, cos_moment=True)
+        direction = torch.where(flux > 0, mom / flux, torch.ones_like(flux))
+        return flux, direction
+
+    def collect_counts(self, rays, wavelength=None, where=True):
+        """``(counts, flux)``: the ray counts and the intensity image."""
         from ._api import collect
 
         return collect(self, rays, wavelength=wavelength, where=where)

@@ -650,3 +650,18 @@ def collect(sensor, rays: dict, wavelength_bins=None):
     counts = np.bincount(flat, minlength=nw * nx * ny).reshape(nw, nx, ny)
     flux = np.bincount(flat, weights=rays["intensity"].ravel()[ok], minlength=nw * nx * ny)
     return counts, flux.reshape(nw, nx, ny)
+
+
+def collect_reference(sensor, rays: dict, wavelength_bins=None):
+    """(image, direction) of optika/sensors/_sensors.py:92-169 for an ideal
+    sensor material: the intensity image and the flux-weighted mean cosine of
+    incidence, -direction . normal with the flat sensor's normal (0, 0, -1)
+    (optika/sensors/materials/_materials.py:1603-1616), 1 where a pixel is
+    empty."""
+    _, image = collect(sensor, rays, wavelength_bins)
+    r2 = dict(rays)
+    r2["intensity"] = rays["intensity"] * rays["dz"]
+    _, moment = collect(sensor, r2, wavelength_bins)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        direction = np.where(image > 0, moment / image, 1.0)
+    return image, direction

@@ -308,17 +308,54 @@ def test_collect_matches_oracle(cuda):
         wavelength=ref["wavelength"], position=V3(ref["px"], ref["py"], ref["pz"]),
         direction=V3(ref["dx"], ref["dy"], ref["dz"]), intensity=ref["intensity"],
         unvignetted=ref["unvignetted"])
-    counts, flux = s.sensor.collect(rays)
+    counts, flux = s.sensor.collect_counts(rays)
     c_ref, f_ref = O.collect(s.sensor, ref)
     ex, ey = O.histogram_edges(s.sensor)
     fx = (ref["px"] - ex[0]) / PIX
     near = np.abs(fx - np.round(fx)) < 1e-3
     assert np.abs(counts.cpu().numpy() - c_ref).sum() <= 2 * near.sum()
     wbins = (540.0, 560.0, 4)
-    cw, fw = s.sensor.collect(rays, wavelength=wbins)
+    cw, fw = s.sensor.collect_counts(rays, wavelength=wbins)
     cw_ref, _ = O.collect(s.sensor, ref, wavelength_bins=wbins)
     assert cw.shape == (4, 1024, 1024)
     assert cw.sum().item() == cw_ref.sum()
+
+
+def test_collect_image_and_direction(cuda):
+    """The reference's (image, direction) pair: intensity image and the
+    flux-weighted mean cosine of incidence per pixel (ideal sensor
+    material), from otx_collect and from the trace kernel's own binning."""
+    s = configs.newtonian()
+    g = f32(configs.newtonian_grid(num_pupil=500))
+    ref = oracle_rayfunction(s, g)
+    rays = ok.rays.RayVectorArray(
+        wavelength=ref["wavelength"], position=V3(ref["px"], ref["py"], ref["pz"]),
+        direction=V3(ref["dx"], ref["dy"], ref["dz"]), intensity=ref["intensity"],
+        unvignetted=ref["unvignetted"])
+    image, direction = s.sensor.collect(rays)
+    i_ref, d_ref = O.collect_reference(s.sensor, ref)
+    image, direction = image.cpu().numpy(), direction.cpu().numpy()
+    c, _ = (t.cpu().numpy() for t in s.sensor.collect_counts(rays))
+    c_ref, _ = O.collect(s.sensor, ref)
+    same = c == c_ref  # pixels whose rays are the same on both sides
+    assert same.mean() > 0.999
+    assert np.allclose(image[same], i_ref[same], rtol=1e-5, atol=1e-6)
+    assert np.allclose(direction[same], d_ref[same], rtol=0, atol=1e-6)
+    assert np.all(direction[i_ref == 0][same[i_ref == 0]] == 1.0)
+    # the trace kernel's binning fills the same moment image
+    V2 = ok.vectors.Cartesian2dVectorArray
+    pt = _api.PreparedTrace(s, wavelength=torch.as_tensor(g["wavelength"], device="cuda"),
+                            field=V2(torch.as_tensor(g["field_x"], device="cuda"),
+                                     torch.as_tensor(g["field_y"], device="cuda")),
+                            pupil=V2(torch.as_tensor(g["pupil_x"], device="cuda"),
+                                     torch.as_tensor(g["pupil_y"], device="cuda")),
+                            image=True)
+    mom = torch.zeros_like(pt.flux)
+    pt.img.cos_moment = mom.data_ptr()
+    pt.run()
+    torch.cuda.synchronize()
+    m_ref = (i_ref * d_ref)[i_ref > 0].sum()
+    assert abs(float(mom.sum()) - m_ref) < 1e-5 * m_ref
 
 
 def test_sag_api(cuda):
