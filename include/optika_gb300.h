@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define OTX_ABI_VERSION 2
+#define OTX_ABI_VERSION 3
 
 #define OTX_MAX_SURFACES 16
 #define OTX_MAX_POLY_TERMS 8
@@ -44,12 +44,14 @@ typedef int32_t otx_status;
 #define OTX_SAG_CONIC 2    /* optika/sags/_conic.py:16             ConicSag     */
 #define OTX_SAG_PARABOLA 3 /* optika/sags/_parabolic.py:14         ParabolicSag */
 #define OTX_SAG_TOROID 4   /* optika/sags/_toroidal.py:14          ToroidalSag  */
+#define OTX_SAG_CYLINDER 5 /* optika/sags/_cylindrical.py:14       CylindricalSag */
 
 #define OTX_MAT_VACUUM 0            /* optika/materials/_materials.py:82  */
 #define OTX_MAT_MIRROR 1            /* optika/materials/_materials.py:161 */
 #define OTX_MAT_GLASS 2             /* optika/materials/_materials.py:309 */
 #define OTX_MAT_MULTILAYER_MIRROR 3 /* optika/materials/_multilayers.py:908 */
 #define OTX_MAT_MULTILAYER_FILM 4   /* optika/materials/_multilayers.py:839 */
+#define OTX_MAT_MEASURED_MIRROR 5   /* optika/materials/_materials.py:177 */
 
 #define OTX_APER_NONE 0
 #define OTX_APER_CIRCULAR 1    /* optika/apertures/_apertures.py:292 */
@@ -67,6 +69,15 @@ typedef int32_t otx_status;
 #define OTX_RULE_CONSTANT 1    /* optika/rulings/_spacing.py:45  */
 #define OTX_RULE_POLY1D 2      /* optika/rulings/_spacing.py:78  */
 #define OTX_RULE_HOLOGRAPHIC 3 /* optika/rulings/_spacing.py:132 */
+
+/* Groove-efficiency models of the rulings (optika/rulings/_rulings.py).  */
+#define OTX_RULE_EFF_IDEAL 0       /* Rulings: rule_efficiency, :225       */
+#define OTX_RULE_EFF_MEASURED 1    /* MeasuredRulings (table), :255        */
+#define OTX_RULE_EFF_SINUSOIDAL 2  /* SinusoidalRulings, :317              */
+#define OTX_RULE_EFF_SQUARE 3      /* SquareRulings, :461                  */
+#define OTX_RULE_EFF_SAWTOOTH 4    /* SawtoothRulings, :618                */
+#define OTX_RULE_EFF_TRIANGULAR 5  /* TriangularRulings, :762              */
+#define OTX_RULE_EFF_RECTANGULAR 6 /* RectangularRulings, :915             */
 
 #define OTX_SYS_FLAG_FINAL_IDENTITY 1 /* final_to_output is the identity */
 
@@ -135,7 +146,7 @@ typedef struct otx_surface {
   /* sag */
   int32_t sag_type;
   float sag_radius;    /* R (sphere), 2f (parabola)                          */
-  float sag_curvature; /* c = 1/R (sphere, conic, toroid minor radius)       */
+  float sag_curvature; /* c = 1/R (sphere, conic, cylinder, toroid minor radius) */
   float sag_conic;     /* k                                                  */
   float sag_radius_of_rotation; /* toroid major radius                       */
   float sag_focal_length;       /* parabola                                  */
@@ -144,6 +155,8 @@ typedef struct otx_surface {
   int32_t mat_type;
   int32_t mat_is_mirror;
   int32_t mat_stack; /* index into otx_system.stacks (multilayer types)      */
+  int32_t mat_table; /* measured mirror: index into tables,
+                        columns [wavelength nm, reflectivity, unused]        */
   float sellmeier_b[3];
   float sellmeier_c[3]; /* nm^2 */
 
@@ -164,6 +177,11 @@ typedef struct otx_surface {
   float holo_x1[3], holo_x2[3];
   float holo_wavelength; /* mm */
   float holo_d1, holo_d2; /* +1 diverging, -1 converging */
+  int32_t rule_eff_type;  /* OTX_RULE_EFF_*                              */
+  int32_t rule_table;     /* measured efficiency: index into tables,
+                             columns [wavelength nm, efficiency, unused] */
+  float rule_depth;       /* groove depth / model amplitude (nm)         */
+  float rule_duty;        /* rectangular: a = 2 pi duty ratio (rad)      */
 
   int32_t is_sensor; /* bin rays leaving this surface (must be the last) */
   int32_t pad_;
@@ -528,6 +546,18 @@ otx_status otx_collect(const otx_sensor* sensor, const otx_rays* rays,
  *         (optika/sags/_abc.py:76-107 intercept and its overrides). */
 otx_status otx_sag_eval(const otx_system* sys, int32_t mode, const otx_rays* in,
                         const otx_rays* out, void* stream);
+
+/* Evaluate the rulings of sys->surfaces[0] for rays at the surface (in the
+ * surface frame) with the sag normals `normal` (normal->dx, dy, dz; the
+ * rays' direction in rays->d*, position in rays->p*, wavelength in nm).
+ * mode 0: groove efficiency into efficiency[count]
+ *         (optika/rulings/_rulings.py:207-222 efficiency and its models)
+ * mode 1: effective incident direction into out->d*
+ *         (optika/rulings/_rulings.py:170-204 incident_effective).
+ * Surfaces without rulings return OTX_ERR_INVALID. */
+otx_status otx_rulings_eval(const otx_system* sys, int32_t mode, const otx_rays* rays,
+                            const otx_rays* normal, float* efficiency, const otx_rays* out,
+                            void* stream);
 
 #ifdef __cplusplus
 }

@@ -8,6 +8,7 @@ device these functions raise.
 from __future__ import annotations
 
 import ctypes
+import dataclasses
 from typing import Sequence
 
 import numpy as np
@@ -468,6 +469,41 @@ def sag_intercept(sag, rays: RayVectorArray) -> RayVectorArray:
                              ctypes.byref(out), stream_handle()), "otx_sag_eval")
     res = _to_ray_array({**b_in, "px": px, "py": py, "pz": pz}, shape)
     return res
+
+
+def rulings_eval(rulings, what: str, rays: RayVectorArray, normal):
+    """Groove efficiency (``what="efficiency"``) or the rays with their
+    effective incident direction (``"incident_effective"``) of ``rulings``
+    for rays at the ruled surface, through otx_rulings_eval."""
+    from .surfaces import Surface
+
+    dev = device()
+    comps = dict(px=rays.position.x, py=rays.position.y, pz=rays.position.z,
+                 dx=rays.direction.x, dy=rays.direction.y, dz=rays.direction.z,
+                 wavelength=rays.wavelength, index_refraction=rays.index_refraction,
+                 nx=normal.x, ny=normal.y, nz=normal.z)
+    ts = {k: as_f32(v, dev) for k, v in comps.items()}
+    shape = tuple(torch.broadcast_shapes(*[t.shape for t in ts.values()]))
+    n = int(np.prod(shape)) if len(shape) else 1
+    b = {k: t.expand(shape).reshape(-1).contiguous() for k, t in ts.items()}
+    lw = lower_surfaces([Surface(rulings=rulings)], pre=np.eye(4), final=None,
+                        input_mode=L.INPUT_RAYS, device=dev)
+    lib = L.load()
+    rs = _rays_struct({k: b[k] for k in ("px", "py", "pz", "dx", "dy", "dz", "wavelength",
+                                         "index_refraction")}, n)
+    ns = _rays_struct(dict(dx=b["nx"], dy=b["ny"], dz=b["nz"]), n)
+    if what == "efficiency":
+        eff = torch.empty(n, dtype=torch.float32, device=dev)
+        L.check(lib.otx_rulings_eval(ctypes.byref(lw.sys), 0, ctypes.byref(rs), ctypes.byref(ns),
+                                     ptr(eff), None, stream_handle()), "otx_rulings_eval")
+        return eff.reshape(shape)
+    dx, dy, dz = (torch.empty(n, dtype=torch.float32, device=dev) for _ in range(3))
+    out = _rays_struct(dict(dx=dx, dy=dy, dz=dz), n)
+    L.check(lib.otx_rulings_eval(ctypes.byref(lw.sys), 1, ctypes.byref(rs), ctypes.byref(ns),
+                                 None, ctypes.byref(out), stream_handle()), "otx_rulings_eval")
+    return dataclasses.replace(
+        rays, direction=Cartesian3dVectorArray(dx.reshape(shape), dy.reshape(shape),
+                                               dz.reshape(shape)))
 
 
 def multilayer_efficiency_gpu(wavelength, direction, n, layers, substrate):

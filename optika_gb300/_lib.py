@@ -10,7 +10,7 @@ from __future__ import annotations
 import ctypes
 import pathlib
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_SURFACES = 16
 MAX_POLY_TERMS = 8
 MAX_VERTICES = 64
@@ -25,14 +25,17 @@ ERR_CUDA = 3
 ERR_SIZE = 4
 ERR_TIMEOUT = 5
 
-SAG_FLAT, SAG_SPHERE, SAG_CONIC, SAG_PARABOLA, SAG_TOROID = range(5)
-MAT_VACUUM, MAT_MIRROR, MAT_GLASS, MAT_MULTILAYER_MIRROR, MAT_MULTILAYER_FILM = range(5)
+SAG_FLAT, SAG_SPHERE, SAG_CONIC, SAG_PARABOLA, SAG_TOROID, SAG_CYLINDER = range(6)
+(MAT_VACUUM, MAT_MIRROR, MAT_GLASS, MAT_MULTILAYER_MIRROR, MAT_MULTILAYER_FILM,
+ MAT_MEASURED_MIRROR) = range(6)
 APER_NONE, APER_CIRCULAR, APER_RECTANGULAR, APER_ELLIPTICAL, APER_SECTOR, APER_POLYGON = range(6)
 APER_FLAG_INVERTED = 1
 APER_FLAG_ACTIVE = 2
 APER_FLAG_DIRECTION = 4
 APER_FLAG_TRANSFORM = 8
 RULE_NONE, RULE_CONSTANT, RULE_POLY1D, RULE_HOLOGRAPHIC = range(4)
+(RULE_EFF_IDEAL, RULE_EFF_MEASURED, RULE_EFF_SINUSOIDAL, RULE_EFF_SQUARE, RULE_EFF_SAWTOOTH,
+ RULE_EFF_TRIANGULAR, RULE_EFF_RECTANGULAR) = range(7)
 INPUT_RAYS, INPUT_GRID_INFINITY, INPUT_GRID_FINITE = range(3)
 EPI_SILU_BF16, EPI_BIAS_F32, EPI_F32, EPI_DSILU_BF16, EPI_F32_ATOMIC = range(5)
 SYS_FLAG_FINAL_IDENTITY = 1
@@ -108,6 +111,7 @@ class Surface(ctypes.Structure):
         ("mat_type", i32),
         ("mat_is_mirror", i32),
         ("mat_stack", i32),
+        ("mat_table", i32),
         ("sellmeier_b", f32 * 3),
         ("sellmeier_c", f32 * 3),
         ("aper_type", i32),
@@ -126,6 +130,10 @@ class Surface(ctypes.Structure):
         ("holo_wavelength", f32),
         ("holo_d1", f32),
         ("holo_d2", f32),
+        ("rule_eff_type", i32),
+        ("rule_table", i32),
+        ("rule_depth", f32),
+        ("rule_duty", f32),
         ("is_sensor", i32),
         ("pad_", i32),
     ]
@@ -367,6 +375,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_collect.restype = i32
     lib.otx_sag_eval.argtypes = [P(System), i32, P(Rays), P(Rays), v]
     lib.otx_sag_eval.restype = i32
+    lib.otx_rulings_eval.argtypes = [P(System), i32, P(Rays), P(Rays), v, P(Rays), v]
+    lib.otx_rulings_eval.restype = i32
 
 
 def load() -> ctypes.CDLL:

@@ -10,6 +10,7 @@ CPU fallback.
 
 from __future__ import annotations
 
+import dataclasses
 import math
 from typing import Sequence
 
@@ -44,6 +45,18 @@ def set_affine(dst: L.Affine, m: np.ndarray) -> None:
     dst.flags = L.AFFINE_ROT_IDENTITY if np.array_equal(r, np.eye(3)) else 0
 
 
+@dataclasses.dataclass(eq=False)
+class _Table:
+    """A measured efficiency in the table pool's [x, y, -] column layout."""
+
+    wavelength: np.ndarray
+    n: np.ndarray
+
+    @property
+    def k(self) -> np.ndarray:
+        return np.zeros_like(self.n)
+
+
 class Lowering:
     """Accumulates the pools (vertices, layers, stacks, tables) of one system."""
 
@@ -61,20 +74,21 @@ class Lowering:
             self.sys.stacks[k].substrate = -1
 
     # ------------------------------------------------------------ layers
+    def _add_table(self, table) -> int:
+        for i, c in enumerate(self.table_list):
+            if c is table:
+                return i
+        if len(self.table_list) >= L.MAX_STACKS * 4:
+            raise ValueError("too many tables (chemicals, measured efficiencies) in one system")
+        self.table_list.append(table)
+        return len(self.table_list) - 1
+
     def _index_source(self, lay: L.Layer, chemical) -> None:
         lay.table = -1
         if chemical is None:
             lay.n_re, lay.n_im = 1.0, 0.0
         elif isinstance(chemical, Chemical):
-            for i, c in enumerate(self.table_list):
-                if c is chemical:
-                    lay.table = i
-                    break
-            else:
-                if len(self.table_list) >= L.MAX_STACKS * 4:
-                    raise ValueError("too many chemical tables in one system")
-                self.table_list.append(chemical)
-                lay.table = len(self.table_list) - 1
+            lay.table = self._add_table(chemical)
         elif isinstance(chemical, str):
             raise NotImplementedError(
                 "chemical formulas need an explicit table: pass "
@@ -185,6 +199,14 @@ class Lowering:
             d.sag_radius = float(sag.radius)
             d.sag_curvature = 1.0 / float(sag.radius)
             d.sag_conic = float(sag.conic)
+        elif isinstance(sag, sg.CylindricalSag):
+            r = float(sag.radius)
+            if math.isinf(r):  # the reference's formulas reduce to the plane
+                d.sag_type = L.SAG_FLAT
+            else:
+                d.sag_type = L.SAG_CYLINDER
+                d.sag_radius = r
+                d.sag_curvature = 1.0 / r
         elif isinstance(sag, sg.ToroidalSag):
             d.sag_type = L.SAG_TOROID
             d.sag_radius = float(sag.radius)
@@ -203,6 +225,11 @@ class Lowering:
         elif isinstance(m, mt.MultilayerFilm):
             d.mat_type = L.MAT_MULTILAYER_FILM
             d.mat_stack = self.add_stack(m.layers, None)
+        elif isinstance(m, mt.MeasuredMirror):
+            wavelength, reflectivity = m.table()
+            d.mat_type = L.MAT_MEASURED_MIRROR
+            d.mat_is_mirror = 1
+            d.mat_table = self._add_table(_Table(wavelength, reflectivity))
         elif isinstance(m, mt.AbstractMirror):
             d.mat_type = L.MAT_MIRROR
             d.mat_is_mirror = 1
@@ -266,12 +293,35 @@ class Lowering:
         if r is None:
             d.rule_type = L.RULE_NONE
             return
-        if not isinstance(r, ru.Rulings):
-            raise NotImplementedError(
-                f"rulings {type(r).__name__} are not supported on the GPU path (only ideal Rulings)"
-            )
+        if not isinstance(r, ru.AbstractRulings):
+            raise NotImplementedError(f"rulings {type(r).__name__} are not supported on the GPU path")
         d.rule_order = float(r.diffraction_order)
-        d.rule_efficiency = float(r.efficiency)
+        d.rule_efficiency = 1.0
+        d.rule_eff_type = L.RULE_EFF_IDEAL
+        if isinstance(r, ru.MeasuredRulings):
+            wavelength, efficiency = r.table()
+            d.rule_eff_type = L.RULE_EFF_MEASURED
+            d.rule_table = self._add_table(_Table(wavelength, efficiency))
+        elif not isinstance(r, ru.Rulings):
+            models = {
+                ru.SinusoidalRulings: L.RULE_EFF_SINUSOIDAL,
+                ru.SquareRulings: L.RULE_EFF_SQUARE,
+                ru.SawtoothRulings: L.RULE_EFF_SAWTOOTH,
+                ru.TriangularRulings: L.RULE_EFF_TRIANGULAR,
+                ru.RectangularRulings: L.RULE_EFF_RECTANGULAR,
+            }
+            if type(r) not in models:
+                raise NotImplementedError(
+                    f"rulings {type(r).__name__} are not supported on the GPU path")
+            d.rule_eff_type = models[type(r)]
+            if d.rule_eff_type == L.RULE_EFF_SINUSOIDAL and (
+                    float(r.diffraction_order) != int(r.diffraction_order)):
+                raise NotImplementedError("sinusoidal rulings need an integer diffraction order")
+            # groove depth (mm) over the model's amplitude, in nm like the
+            # wavelengths it is divided by
+            d.rule_depth = float(r.depth) / float(r.amplitude) * 1e6
+            if isinstance(r, ru.RectangularRulings):
+                d.rule_duty = 2 * math.pi * float(r.ratio_duty)
         s = r.spacing_
         if isinstance(s, ru.ConstantRulingSpacing):
             d.rule_type = L.RULE_CONSTANT

@@ -83,6 +83,39 @@ __global__ void k_sag(const __grid_constant__ otx_system sys, const int mode,
   }
 }
 
+// mode 0: groove efficiency -> eff ; 1: effective incident direction -> out.d*
+__global__ void k_rulings(const __grid_constant__ otx_system sys, const int mode,
+                          const otx_rays r, const otx_rays nrm, float* eff,
+                          const otx_rays out) {
+  const otx_surface& s = sys.surfaces[0];
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < r.count; i += step) {
+    Ray q;
+    q.px = reinterpret_cast<const float*>(r.px)[i];
+    q.py = reinterpret_cast<const float*>(r.py)[i];
+    q.pz = reinterpret_cast<const float*>(r.pz)[i];
+    q.dx = reinterpret_cast<const float*>(r.dx)[i];
+    q.dy = reinterpret_cast<const float*>(r.dy)[i];
+    q.dz = reinterpret_cast<const float*>(r.dz)[i];
+    q.wl = reinterpret_cast<const float*>(r.wavelength)[i];
+    q.n = r.index_refraction ? reinterpret_cast<const float*>(r.index_refraction)[i] : 1.f;
+    const float nx = reinterpret_cast<const float*>(nrm.dx)[i];
+    const float ny = reinterpret_cast<const float*>(nrm.dy)[i];
+    const float nz = reinterpret_cast<const float*>(nrm.dz)[i];
+    if (mode == 0) {
+      eff[i] = (s.rule_eff_type == OTX_RULE_EFF_IDEAL)
+                   ? s.rule_efficiency
+                   : ruling_efficiency_call(sys, s, s.rule_type, q.px, q.py, q.pz, q.dx, q.dy,
+                                            q.dz, q.wl, nx, ny, nz);
+    } else {
+      incident_effective(s.rule_type, s, q, nx, ny, nz);
+      reinterpret_cast<float*>(out.dx)[i] = q.dx;
+      reinterpret_cast<float*>(out.dy)[i] = q.dy;
+      reinterpret_cast<float*>(out.dz)[i] = q.dz;
+    }
+  }
+}
+
 static int grid_for(int64_t n) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -119,7 +152,7 @@ extern "C" otx_status otx_sag_eval(const otx_system* sys, int32_t mode, const ot
   if (!sys || sys->abi_version != OTX_ABI_VERSION || !in || !out) return OTX_ERR_INVALID;
   if (mode < 0 || mode > 2) return OTX_ERR_INVALID;
   const int st = sys->surfaces[0].sag_type;
-  if (st < OTX_SAG_FLAT || st > OTX_SAG_TOROID) return OTX_ERR_UNSUPPORTED;
+  if (st < OTX_SAG_FLAT || st > OTX_SAG_CYLINDER) return OTX_ERR_UNSUPPORTED;
   if (in->count < 0) return OTX_ERR_INVALID;
   if (in->count == 0) return OTX_OK;
   if (!in->px || !in->py) return OTX_ERR_INVALID;
@@ -129,5 +162,27 @@ extern "C" otx_status otx_sag_eval(const otx_system* sys, int32_t mode, const ot
     return OTX_ERR_INVALID;
   k_sag<<<grid_for(in->count), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*sys, mode, *in,
                                                                                *out);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+extern "C" otx_status otx_rulings_eval(const otx_system* sys, int32_t mode, const otx_rays* rays,
+                                       const otx_rays* normal, float* efficiency,
+                                       const otx_rays* out, void* stream) {
+  if (!sys || !rays || !normal) return OTX_ERR_INVALID;
+  if (mode < 0 || mode > 1) return OTX_ERR_INVALID;
+  otx_system one = *sys;
+  one.num_surfaces = 1;
+  if (const otx_status vs = validate_system(&one)) return vs;
+  if (sys->surfaces[0].rule_type == OTX_RULE_NONE) return OTX_ERR_INVALID;
+  if (rays->count < 0) return OTX_ERR_INVALID;
+  if (rays->count == 0) return OTX_OK;
+  if (!rays->px || !rays->py || !rays->pz || !rays->dx || !rays->dy || !rays->dz ||
+      !rays->wavelength || !normal->dx || !normal->dy || !normal->dz)
+    return OTX_ERR_INVALID;
+  if (mode == 0 && !efficiency) return OTX_ERR_INVALID;
+  if (mode == 1 && (!out || !out->dx || !out->dy || !out->dz)) return OTX_ERR_INVALID;
+  const otx_rays none{};
+  k_rulings<<<grid_for(rays->count), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      *sys, mode, *rays, *normal, efficiency, mode == 1 ? *out : none);
   return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
 }

@@ -113,8 +113,7 @@ extern "C" otx_status otx_trace_batch(const otx_system* base, const otx_batch* b
                                       const otx_rays* out, const otx_image* image,
                                       const otx_launch* launch, void* stream) {
   if (!base || !batch || !out) return OTX_ERR_INVALID;
-  if (base->abi_version != OTX_ABI_VERSION) return OTX_ERR_INVALID;
-  if (base->num_surfaces < 1 || base->num_surfaces > OTX_MAX_SURFACES) return OTX_ERR_SIZE;
+  if (const otx_status vs = validate_system(base)) return vs;
   if (base->input_mode != OTX_INPUT_GRID_INFINITY) return OTX_ERR_INVALID;
   // rays are stored in the last surface's frame: it must be the output frame
   if (!(base->flags & OTX_SYS_FLAG_FINAL_IDENTITY)) return OTX_ERR_UNSUPPORTED;
@@ -250,8 +249,7 @@ extern "C" otx_status otx_trace_batch_noalloc(const otx_system* base, const otx_
                                               const otx_rays* out, const otx_image* image,
                                               const otx_launch* launch, void* stream) {
   if (!base || !batch || !out) return OTX_ERR_INVALID;
-  if (base->abi_version != OTX_ABI_VERSION) return OTX_ERR_INVALID;
-  if (base->num_surfaces < 1 || base->num_surfaces > OTX_MAX_SURFACES) return OTX_ERR_SIZE;
+  if (const otx_status vs = validate_system(base)) return vs;
   if (base->input_mode != OTX_INPUT_GRID_INFINITY) return OTX_ERR_INVALID;
   // rays are stored in the last surface's frame: it must be the output frame
   if (!(base->flags & OTX_SYS_FLAG_FINAL_IDENTITY)) return OTX_ERR_UNSUPPORTED;

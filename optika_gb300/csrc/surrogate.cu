@@ -311,8 +311,7 @@ otx_status otx_surrogate_image(const otx_system* base, const otx_batch* batch,
                                const otx_image* image, unsigned long long* stats, void* stream) {
   if (!base || !batch_ok(batch, sg) || first < 0 || count < 0 || !y || ldy < 3 || !aux || !stats)
     return OTX_ERR_INVALID;
-  if (base->abi_version != OTX_ABI_VERSION) return OTX_ERR_INVALID;
-  if (base->num_surfaces < 1 || base->num_surfaces > OTX_MAX_SURFACES) return OTX_ERR_SIZE;
+  if (const otx_status vs = validate_system(base)) return vs;
   if (base->input_mode != OTX_INPUT_GRID_INFINITY) return OTX_ERR_INVALID;
   // predicted positions are in the output frame, binning in the sensor's
   if (!(base->flags & OTX_SYS_FLAG_FINAL_IDENTITY)) return OTX_ERR_UNSUPPORTED;

@@ -485,9 +485,8 @@ otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* ba
   if (b.num_configs < 1 || !b.ray_offset || sg->num_configs != b.num_configs ||
       !sg->config_inputs || !sg->baseline || !(sg->out_scale > 0.f))
     return OTX_ERR_INVALID;
-  if (base->abi_version != OTX_ABI_VERSION || base->input_mode != OTX_INPUT_GRID_INFINITY)
-    return OTX_ERR_INVALID;
-  if (base->num_surfaces < 1 || base->num_surfaces > OTX_MAX_SURFACES) return OTX_ERR_SIZE;
+  if (const otx_status vs = validate_system(base)) return vs;
+  if (base->input_mode != OTX_INPUT_GRID_INFINITY) return OTX_ERR_INVALID;
   if (!(base->flags & OTX_SYS_FLAG_FINAL_IDENTITY)) return OTX_ERR_UNSUPPORTED;
   if (b.num_overrides < 0 || b.num_overrides > OTX_BATCH_MAX_OVERRIDES) return OTX_ERR_SIZE;
   for (int j = 0; j < b.num_overrides; ++j)

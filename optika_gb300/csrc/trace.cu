@@ -25,15 +25,19 @@ static int num_sms() {
   return g_num_sms;
 }
 
-static otx_status validate_system(const otx_system* sys) {
+otx_status validate_system(const otx_system* sys) {
   if (!sys) return OTX_ERR_INVALID;
   if (sys->abi_version != OTX_ABI_VERSION) return OTX_ERR_INVALID;
   if (sys->num_surfaces < 1 || sys->num_surfaces > OTX_MAX_SURFACES) return OTX_ERR_SIZE;
   for (int i = 0; i < sys->num_surfaces; ++i) {
     const otx_surface& s = sys->surfaces[i];
-    if (s.sag_type < OTX_SAG_FLAT || s.sag_type > OTX_SAG_TOROID) return OTX_ERR_UNSUPPORTED;
-    if (s.mat_type < OTX_MAT_VACUUM || s.mat_type > OTX_MAT_MULTILAYER_FILM)
+    if (s.sag_type < OTX_SAG_FLAT || s.sag_type > OTX_SAG_CYLINDER) return OTX_ERR_UNSUPPORTED;
+    if (s.mat_type < OTX_MAT_VACUUM || s.mat_type > OTX_MAT_MEASURED_MIRROR)
       return OTX_ERR_UNSUPPORTED;
+    if (s.mat_type == OTX_MAT_MEASURED_MIRROR &&
+        (s.mat_table < 0 || s.mat_table >= OTX_MAX_STACKS * 4 ||
+         sys->tables[s.mat_table].count < 1 || sys->table_data == 0))
+      return OTX_ERR_INVALID;
     if (s.aper_type < OTX_APER_NONE || s.aper_type > OTX_APER_POLYGON) return OTX_ERR_UNSUPPORTED;
     if (s.rule_type < OTX_RULE_NONE || s.rule_type > OTX_RULE_HOLOGRAPHIC)
       return OTX_ERR_UNSUPPORTED;
@@ -48,6 +52,14 @@ static otx_status validate_system(const otx_system* sys) {
     if (s.rule_type == OTX_RULE_POLY1D &&
         (s.rule_num_terms < 0 || s.rule_num_terms > OTX_MAX_POLY_TERMS))
       return OTX_ERR_SIZE;
+    if (s.rule_type != OTX_RULE_NONE) {
+      if (s.rule_eff_type < OTX_RULE_EFF_IDEAL || s.rule_eff_type > OTX_RULE_EFF_RECTANGULAR)
+        return OTX_ERR_UNSUPPORTED;
+      if (s.rule_eff_type == OTX_RULE_EFF_MEASURED &&
+          (s.rule_table < 0 || s.rule_table >= OTX_MAX_STACKS * 4 ||
+           sys->tables[s.rule_table].count < 1 || sys->table_data == 0))
+        return OTX_ERR_INVALID;
+    }
   }
   for (int k = 0; k < OTX_MAX_STACKS; ++k) {
     const otx_stack& K = sys->stacks[k];

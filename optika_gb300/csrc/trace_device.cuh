@@ -166,6 +166,15 @@ __device__ __forceinline__ float sag_eval(int sag_type, const otx_surface& s, fl
       gy = cg * y;
       return c * r2 / (1.f + g);
     }
+    case OTX_SAG_CYLINDER: {
+      // optika/sags/_cylindrical.py:75-91: z = c x^2 / (1 + sqrt(1 - c^2 x^2))
+      const float c = s.sag_curvature;
+      const float x2 = x * x;
+      const float g = sqrtf(1.f - c * c * x2);
+      gx = c * x / g;
+      gy = 0.f;
+      return c * x2 / (1.f + g);
+    }
     case OTX_SAG_TOROID: {
       const float c = s.sag_curvature;
       const float r = s.sag_radius_of_rotation;
@@ -216,6 +225,10 @@ __device__ __forceinline__ float newton_step(int sag_type, const otx_surface& s,
 //             linear form when u_x^2 + u_y^2 <= 1e-10)
 //   toroid    optika/sags/_abc.py:76-107 (iterative root near the vertex
 //             plane; here Newton from the plane intercept)
+//   cylinder  optika/sags/_cylindrical.py:115-160 (circle of radius R about
+//             the y axis through (0, 0, R): the -sign(R u_z) root of
+//             (u_x^2 + u_z^2) t^2 + 2 hb t + cc = 0, and the vertex-plane
+//             intercept -o_z / u_z when the discriminant is not positive)
 // The closed forms use the cancellation-free product-of-roots identity.
 //
 // The direction's low parts (lx, ly, lz) enter only the intercept point
@@ -241,6 +254,7 @@ __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
     return t - dt;
   }
   float t;
+  bool polish = true;
   switch (sag_type) {
     case OTX_SAG_SPHERE: {
       const float R = s.sag_radius;
@@ -309,6 +323,27 @@ __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
       }
       break;
     }
+    case OTX_SAG_CYLINDER: {
+      const float R = s.sag_radius;
+      const float a = fmaf(ux, ux, uz * uz);
+      const float hb = fmaf(ux, oxf, uz * (ozf - R));
+      const float cc = fmaf(oxf, oxf, ozf * (ozf - 2.f * R));
+      const float disc = fmaf(hb, hb, -a * cc);
+      if (disc > 0.f) {
+        const float q = sqrtf(disc);
+        const float sg = sgnf(R * uz);
+        // chosen root (-hb - sg q) / a ; the other (-hb + sg q) / a ;
+        // their product cc / a
+        if (sg != 0.f && sgnf(-hb) == sg)
+          t = cc / (-hb + sg * q);
+        else
+          t = (-hb - sg * q) / a;
+      } else {
+        t = -ozf / uz;
+        polish = false;  // the reference keeps the vertex-plane point
+      }
+      break;
+    }
     default:  // toroid: start from the vertex plane
       t = -ozf / uz;
       break;
@@ -331,7 +366,7 @@ __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
     if (!conv) {
       x = y = z = NAN;
     }
-  } else if (isfinite(t)) {
+  } else if (polish && isfinite(t)) {
     t -= newton_step(sag_type, s, x, y, z, ux, uy, uz);
   }
   return t;
@@ -343,6 +378,7 @@ __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
 //   conic    optika/sags/_conic.py:50-75
 //   parabola optika/sags/_parabolic.py:40-63 (equal to the k = -1 conic)
 //   toroid   optika/sags/_toroidal.py:59-88
+//   cylinder optika/sags/_cylindrical.py:93-113 (x / R, 0, -sqrt(1 - (x/R)^2))
 //
 // v receives a vector parallel to the normal that is exact up to the
 // rounding of its components (the unnormalised gradient (g_x, g_y, -1), or
@@ -355,6 +391,15 @@ __device__ __forceinline__ void normal(int sag_type, const otx_surface& s, float
       nx = c * x;
       ny = c * y;
       nz = -sqrtf(1.f - nx * nx - ny * ny);
+      v[0] = nx;
+      v[1] = ny;
+      v[2] = nz;
+      return;
+    }
+    case OTX_SAG_CYLINDER: {
+      nx = s.sag_curvature * x;
+      ny = 0.f;
+      nz = -sqrtf(1.f - nx * nx);
       v[0] = nx;
       v[1] = ny;
       v[2] = nz;
@@ -611,6 +656,136 @@ __device__ __forceinline__ void incident_effective(int rule_type, const otx_surf
   r.dx = fmaf(f, kx, r.dx);
   r.dy = fmaf(f, ky, r.dy);
   r.dz = fmaf(f, kz, r.dz);
+}
+
+// Bessel function of the first kind J_m(x) for an integer order m (any
+// sign) and a real argument of any sign, from CUDA's jnf of order |m| at
+// |x|: J_-m(x) = (-1)^m J_m(x) and J_m(-x) = (-1)^m J_m(x).
+__device__ __forceinline__ float bessel_j(float order, float x) {
+  const int m = (int)order;
+  const int am = m < 0 ? -m : m;
+  float j = jnf(am, fabsf(x));
+  if ((am & 1) && ((m < 0) != (x < 0.f))) j = -j;
+  return j;
+}
+
+// Python's i % 2 == 0 for a float order (floored modulo).
+__device__ __forceinline__ bool order_even(float m) {
+  return m - 2.f * floorf(0.5f * m) == 0.f;
+}
+
+// numpy.interp of the second column of a [x(n), y(n), -] table (clamped to
+// the end values outside the table).
+__device__ __forceinline__ float table_interp(const otx_system& sys, int table, float x) {
+  const otx_table T = sys.tables[table];
+  const float* xs = reinterpret_cast<const float*>(sys.table_data) + T.offset;
+  const float* ys = xs + T.count;
+  const int cnt = T.count;
+  if (!(x > xs[0])) return ys[0];
+  if (!(x < xs[cnt - 1])) return ys[cnt - 1];
+  int lo = 0, hi = cnt - 1;  // xs[lo] < x < xs[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (xs[mid] <= x)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  const float w = (x - xs[lo]) / (xs[hi] - xs[lo]);
+  return fmaf(w, ys[hi] - ys[lo], ys[lo]);
+}
+
+// table_interp behind the checks of the table index the host also makes
+// (NaN for an unusable table).
+__device__ __forceinline__ float table_value(const otx_system& sys, int table, float x) {
+  if (table < 0 || table >= OTX_MAX_STACKS * 4 || sys.tables[table].count < 1 ||
+      sys.table_data == 0)
+    return NAN;
+  return table_interp(sys, table, x);
+}
+
+// Groove efficiency of the ruling models, on the rays after
+// incident_effective (optika/surfaces.py:182-184) at the intercept point
+// (px, py, pz) with effective direction a = (dx, dy, dz) and sag normal n:
+//   measured     optika/rulings/_rulings.py:287-314 (interp on wavelength)
+//   sinusoidal   :404-457   J_m(2 gamma)
+//   square       :548-614   cos^2(pi g / 2) (m = 0), 0 (m even),
+//                           (2 sin(pi g / 2) / (m pi))^2 (m odd)
+//   sawtooth     :705-758   (sin(pi g) / (pi (g + m)))^2
+//   triangular   :849-911   (g / ((pi g / 2)^2 + m^2))^2 times
+//                           sin^2 (m even) or cos^2 (m odd) of pi^2 g / 4
+//   rectangular  :1008-1073 b = sin^2(pi g / sqrt(2 (1 - cos a))),
+//                           1 - (2 a / pi - (a / pi)^2) b (m = 0),
+//                           2 (1 - cos(m a)) b / (m pi)^2 otherwise
+// with, as in the reference, q = normalize(n x kappa), s = a.q,
+// cos_theta = -(a - s).n where the scalar s is subtracted from every
+// component of a, and g = pi depth / (lambda cos_theta), depth being the
+// groove depth over the model's amplitude (folded in by the host).
+static __device__ __noinline__ float ruling_efficiency_call(const otx_system& sys,
+                                                            const otx_surface& s, int rule_type,
+                                                            float px, float py, float pz,
+                                                            float dx, float dy, float dz,
+                                                            float wl, float nx, float ny,
+                                                            float nz) {
+  const int model = s.rule_eff_type;
+  if (model == OTX_RULE_EFF_MEASURED) return table_value(sys, s.rule_table, wl);
+  float kx, ky, kz;
+  ruling_kappa(rule_type, s, px, py, pz, nx, ny, nz, kx, ky, kz);
+  float qx = ny * kz - nz * ky;
+  float qy = nz * kx - nx * kz;
+  float qz = nx * ky - ny * kx;
+  const float qi = 1.f / sqrtf(qx * qx + qy * qy + qz * qz);
+  qx *= qi;
+  qy *= qi;
+  qz *= qi;
+  const float sp = dx * qx + dy * qy + dz * qz;
+  const float cos_t = -((dx - sp) * nx + (dy - sp) * ny + (dz - sp) * nz);
+  const float pi = 3.14159265358979f;
+  const float g = pi * s.rule_depth / (wl * cos_t);
+  const float m = s.rule_order;
+  switch (model) {
+    case OTX_RULE_EFF_SINUSOIDAL:
+      return bessel_j(m, 2.f * g);
+    // sin(pi x) and cos(pi x) as sinpif / cospif: no rounding of pi x
+    case OTX_RULE_EFF_SQUARE: {
+      if (m == 0.f) {
+        const float c = cospif(0.5f * g);
+        return c * c;
+      }
+      if (order_even(m)) return 0.f;
+      const float v = 2.f * sinpif(0.5f * g) / (m * pi);
+      return v * v;
+    }
+    case OTX_RULE_EFF_SAWTOOTH: {
+      const float u = g + m;
+      float v;
+      if (m == rintf(m)) {
+        // sin(pi g) = (-1)^m sin(pi u): sinc^2(u), well conditioned near
+        // the blaze u -> 0 where the quotient tends to 1
+        v = (u == 0.f) ? 1.f : sinpif(u) / (pi * u);
+      } else {
+        v = sinpif(g) / (pi * u);
+      }
+      return v * v;
+    }
+    case OTX_RULE_EFF_TRIANGULAR: {
+      const float h = 0.5f * pi * g;
+      const float a = g / fmaf(h, h, m * m);
+      const float ph = 0.25f * pi * g;  // (pi^2 g / 4) / pi
+      const float v = a * (order_even(m) ? sinpif(ph) : cospif(ph));
+      return v * v;
+    }
+    case OTX_RULE_EFF_RECTANGULAR: {
+      const float a = s.rule_duty;
+      const float b0 = sinpif(g / sqrtf(2.f * (1.f - cosf(a))));
+      const float b = b0 * b0;
+      if (m == 0.f) return 1.f - (2.f * a / pi - (a / pi) * (a / pi)) * b;
+      const float mp = m * pi;
+      return 2.f / (mp * mp) * (1.f - cosf(m * a)) * b;
+    }
+    default:
+      return s.rule_efficiency;
+  }
 }
 
 // ---------------------------------------------------------------- apertures
@@ -1047,6 +1222,12 @@ __device__ __forceinline__ void propagate_surface(const otx_system& sys,
     case OTX_MAT_MIRROR:
       mirror = true;
       break;
+    case OTX_MAT_MEASURED_MIRROR:
+      // optika/materials/_materials.py:279-306: reflectivity interpolated in
+      // the wavelength of the incident rays; n and attenuation unchanged
+      mirror = true;
+      eff = table_value(sys, s.mat_table, r.wl);
+      break;
     case OTX_MAT_GLASS: {
       // Sellmeier, optika/materials/_materials.py:428-438
       const float w2 = r.wl * r.wl;
@@ -1074,7 +1255,11 @@ __device__ __forceinline__ void propagate_surface(const otx_system& sys,
     default:
       break;
   }
-  if (rule_type != OTX_RULE_NONE) eff *= s.rule_efficiency;
+  if (rule_type != OTX_RULE_NONE)
+    eff *= (s.rule_eff_type == OTX_RULE_EFF_IDEAL)
+               ? s.rule_efficiency
+               : ruling_efficiency_call(sys, s, rule_type, r.px, r.py, r.pz, r.dx, r.dy, r.dz,
+                                        r.wl, nx, ny, nz);
   // wavelength_2 = wavelength_1 / (n1 / n2)   (surfaces.py:162-165)
   if (n2 != n1) r.wl = r.wl / (n1 / n2);
   if (mirror && sag_type != OTX_SAG_FLAT && rule_type == OTX_RULE_NONE &&

@@ -14,6 +14,10 @@ __host__ __device__ __forceinline__ bool image_any(const otx_image& img) {
   return img.counts != 0 || img.flux != 0 || img.cos_moment != 0;
 }
 
+// Checks of a system descriptor shared by every entry point that traces
+// through it: type tags, pool indices and sizes (OTX_OK when usable).
+otx_status validate_system(const otx_system* sys);
+
 struct TraceArgs {
   otx_rays in;
   otx_grid grid;

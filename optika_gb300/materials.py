@@ -23,6 +23,7 @@ __all__ = [
     "Vacuum",
     "AbstractMirror",
     "Mirror",
+    "MeasuredMirror",
     "Glass",
     "Layer",
     "LayerSequence",
@@ -55,6 +56,27 @@ class Mirror(AbstractMirror):
     """A perfect mirror, efficiency 1 (optika/materials/_materials.py:161-173)."""
 
     substrate: None | "Layer" = None
+
+
+@dataclasses.dataclass(eq=False)
+class MeasuredMirror(AbstractMirror):
+    """A mirror whose reflectivity was measured at a set of wavelengths for
+    one incidence direction (optika/materials/_materials.py:177-306): linear
+    interpolation in the wavelength of the incident rays, clamped to the end
+    values outside the measured range.  ``efficiency_measured`` is a
+    :class:`~optika_gb300.vectors.FunctionArray` of reflectivities over a
+    :class:`~optika_gb300.vectors.SpectralDirectionalVectorArray` (one
+    increasing wavelength axis in nm, a single direction)."""
+
+    efficiency_measured: object = None
+    substrate: None | "Layer" = None
+    serial_number: None | str = None
+
+    def table(self):
+        """(wavelength, reflectivity) of the measurement."""
+        from .vectors import spectral_table
+
+        return spectral_table(self.efficiency_measured)
 
 
 @dataclasses.dataclass(eq=False)

@@ -22,6 +22,7 @@ __all__ = [
     "ConicSag",
     "ParabolicSag",
     "ToroidalSag",
+    "CylindricalSag",
 ]
 
 
@@ -114,3 +115,17 @@ class ToroidalSag(AbstractSag):
 
     radius: float = math.inf
     radius_of_rotation: float = 0.0
+
+
+@dataclasses.dataclass(eq=False)
+class CylindricalSag(AbstractSag):
+    """``z = c x^2 / (1 + sqrt(1 - c^2 x^2))``: a cylinder of ``radius`` whose
+    axis is parallel to the local y axis (optika/sags/_cylindrical.py:14-160).
+    Rays that miss the cylinder stop at the vertex plane z = 0, as in the
+    reference."""
+
+    radius: float = math.inf
+
+    @property
+    def curvature(self) -> float:
+        return 1.0 / self.radius

@@ -3,7 +3,9 @@
 Components are anything array-like (floats, numpy arrays, torch tensors);
 they are broadcast and moved to the device when a trace is launched.
 Mirrors optika/vectors (ObjectVectorArray ``_vectors_object.py:136-160``,
-PolarizationVectorArray ``_vectors_polarization.py:36-37``).
+PolarizationVectorArray ``_vectors_polarization.py:36-37``) and the two
+named_arrays containers a measured ruling efficiency is given in
+(``SpectralDirectionalVectorArray`` inputs of a ``FunctionArray``).
 """
 
 from __future__ import annotations
@@ -11,11 +13,16 @@ from __future__ import annotations
 import dataclasses
 from typing import Any
 
+import numpy as np
+
 __all__ = [
     "Cartesian2dVectorArray",
     "Cartesian3dVectorArray",
     "ObjectVectorArray",
     "PolarizationVectorArray",
+    "SpectralDirectionalVectorArray",
+    "FunctionArray",
+    "spectral_table",
 ]
 
 
@@ -58,3 +65,39 @@ class PolarizationVectorArray:
     @property
     def average(self) -> Any:
         return (self.s + self.p) / 2
+
+
+@dataclasses.dataclass
+class SpectralDirectionalVectorArray:
+    """A wavelength (nm) and a propagation direction."""
+
+    wavelength: Any = 550.0
+    direction: Any = None
+
+
+@dataclasses.dataclass
+class FunctionArray:
+    """Sampled function: ``outputs`` at ``inputs``."""
+
+    inputs: Any = None
+    outputs: Any = None
+
+
+def spectral_table(measurement: FunctionArray) -> tuple[np.ndarray, np.ndarray]:
+    """(wavelength, value) of a measurement taken at one incidence
+    direction, checked as the reference checks its measured mirrors and
+    rulings (optika/materials/_materials.py:285-301,
+    optika/rulings/_rulings.py:293-307)."""
+    wavelength = np.asarray(measurement.inputs.wavelength, dtype=np.float64)
+    direction = measurement.inputs.direction
+    size = 1 if direction is None else np.asarray(getattr(direction, "x", direction)).size
+    if size != 1:
+        raise ValueError("Interpolating over different incidence angles is not supported.")
+    if wavelength.ndim != 1:
+        raise ValueError(f"wavelength must be one dimensional, got shape {wavelength.shape}")
+    value = np.asarray(measurement.outputs, dtype=np.float64).reshape(-1)
+    if value.shape != wavelength.shape:
+        raise ValueError("one measured value per wavelength is needed")
+    if wavelength.size < 1:
+        raise ValueError("the measurement has no wavelengths")
+    return wavelength, value

@@ -95,6 +95,10 @@ def sag_value(sag, x, y):
         r = sag.radius_of_rotation
         zy = c * y * y / (1 + np.sqrt(1 - c * c * y * y))
         return r - np.sqrt(np.square(r - zy) - x * x)
+    if k == "CylindricalSag":  # _cylindrical.py:75-91
+        c = 1 / sag.radius
+        r2 = x * x
+        return c * r2 / (1 + np.sqrt(1 - c * c * r2)) + 0 * y
     raise NotImplementedError(k)
 
 
@@ -109,6 +113,9 @@ def sag_normal(sag, x, y):
         c = 1 / sag.radius
         nx, ny = c * x, c * y
         return nx, ny, -np.sqrt(1 - nx * nx - ny * ny)
+    if k == "CylindricalSag":  # _cylindrical.py:93-113
+        nx = x / sag.radius
+        return nx, 0 * y, -np.sqrt(1 - nx**2)
     if k == "ParabolicSag":
         r = sag.radius
         s = np.sqrt((x / r) ** 2 + (y / r) ** 2 + 1)
@@ -140,6 +147,7 @@ def sag_intercept(sag, o, u, newton_tol=1e-12, newton_max=60):
     parabola  _parabolic.py:65-158
     toroid    _abc.py:76-107 (iterative root; here Newton from the vertex
               plane intercept, iterated to convergence in float64)
+    cylinder  _cylindrical.py:115-160
     """
     ox, oy, oz = o
     ux, uy, uz = u
@@ -152,6 +160,17 @@ def sag_intercept(sag, o, u, newton_tol=1e-12, newton_max=60):
             px, py, pz = ox, oy, oz - r
             b = ux * px + uy * py + uz * pz
             return -b - np.sign(r * uz) * np.sqrt(b * b - (px * px + py * py + pz * pz - r * r))
+        if k == "CylindricalSag":
+            # line o + d u against the cylinder of radius r about the y axis
+            # through (0, 0, r): b = (0, 0, r) - o, a = y
+            r = sag.radius
+            bx, bz = -ox, r - oz
+            cx, cz = -uz, ux  # u x a
+            ncs = cx * cx + cz * cz
+            negative_b = cx * (-bz) + cz * bx  # (u x a) . (b x a)
+            disc = ncs * r * r - np.square(bx * cx + bz * cz)
+            sgn = np.sign(r * uz)
+            return np.where(disc > 0, (negative_b - sgn * np.sqrt(disc)) / ncs, -oz / uz)
         if k == "ParabolicSag":
             f = sag.focal_length
             a = ux * ux + uy * uy
@@ -295,6 +314,65 @@ def incident_effective(rays, rulings, nx, ny, nz):
     r["dy"] = rays["dy"] + f * gy
     r["dz"] = rays["dz"] + f * gz
     return r
+
+
+def ruling_efficiency(rulings, rays, nx, ny, nz):
+    """Groove efficiency of the ruling models on the rays after
+    incident_effective (optika/surfaces.py:182-184):
+    Rulings :246-251 (1), MeasuredRulings :287-314 (np.interp on wavelength),
+    SinusoidalRulings :404-457, SquareRulings :548-614,
+    SawtoothRulings :705-758, TriangularRulings :849-911,
+    RectangularRulings :1008-1073 of optika/rulings/_rulings.py.  As in the
+    reference, the scalar direction . parallel_rulings is subtracted from
+    every component of the direction before cos_theta = -direction . normal,
+    and the Sinusoidal model returns J_m(2 gamma) itself."""
+    import scipy.special
+
+    name = type(rulings).__name__
+    if name == "Rulings":
+        return 1.0
+    if name == "MeasuredRulings":
+        m = rulings.efficiency_measured
+        return np.interp(rays["wavelength"], np.asarray(m.inputs.wavelength, dtype=np.float64),
+                         np.asarray(m.outputs, dtype=np.float64).reshape(-1))
+    kx, ky, kz = ruling_kappa(spacing_of(rulings), rays["px"], rays["py"], rays["pz"],
+                              nx, ny, nz)
+    with np.errstate(all="ignore"):
+        kl = np.sqrt(kx * kx + ky * ky + kz * kz)
+        kx, ky, kz = kx / kl, ky / kl, kz / kl
+        px, py, pz = ny * kz - nz * ky, nz * kx - nx * kz, nx * ky - ny * kx
+        pl = np.sqrt(px * px + py * py + pz * pz)
+        px, py, pz = px / pl, py / pl, pz / pl
+        dx, dy, dz = rays["dx"], rays["dy"], rays["dz"]
+        s = dx * px + dy * py + dz * pz
+        dx, dy, dz = dx - s, dy - s, dz - s
+        cos_theta = -(dx * nx + dy * ny + dz * nz)
+        wavelength = rays["wavelength"]
+        i = rulings.diffraction_order
+        depth = rulings.depth * 1e6  # mm -> nm
+        if name == "SinusoidalRulings":
+            gamma = np.pi * depth / (wavelength * cos_theta)
+            return scipy.special.jv(i, 2 * gamma)
+        if name == "SquareRulings":
+            gamma = np.pi * (depth / (np.pi / 4)) / (wavelength * cos_theta)
+            result = np.where(i % 2 == 0, 0, np.square(2 * np.sin(np.pi * gamma / 2) / (i * np.pi)))
+            return np.where(i == 0, np.square(np.cos(np.pi * gamma / 2)), result)
+        if name == "SawtoothRulings":
+            gamma = np.pi * (depth / (np.pi / 2)) / (wavelength * cos_theta)
+            return np.square(np.sin(np.pi * gamma) / (np.pi * (gamma + i)))
+        if name == "TriangularRulings":
+            gamma = np.pi * (depth / (np.square(np.pi) / 8)) / (wavelength * cos_theta)
+            a = gamma / (np.square(np.pi * gamma / 2) + np.square(i))
+            return np.where(i % 2 == 0, np.square(a * np.sin(np.square(np.pi) * gamma / 4)),
+                            np.square(a * np.cos(np.square(np.pi) * gamma / 4)))
+        if name == "RectangularRulings":
+            a = 2 * np.pi * rulings.ratio_duty
+            amplitude = np.pi / (2 * np.sqrt(2 * (1 - np.cos(a))))
+            gamma = np.pi * (depth / amplitude) / (wavelength * cos_theta)
+            b = np.square(np.sin(np.pi * gamma / np.sqrt(2 * (1 - np.cos(a)))))
+            return np.where(i == 0, 1 - ((2 * a / np.pi) - np.square(a / np.pi)) * b,
+                            (2 / np.square(i * np.pi)) * (1 - np.cos(i * a)) * b)
+    raise NotImplementedError(name)
 
 
 # ---------------------------------------------------------------- apertures
@@ -521,13 +599,19 @@ def propagate_surface(surface, rays: dict) -> dict:
                 mat.substrate if name == "MultilayerMirror" else None,
             )
         eff = (Rs + Rp) / 2 if name == "MultilayerMirror" else (Ts + Tp) / 2
+    elif name == "MeasuredMirror":  # _materials.py:279-306
+        n2 = n1
+        att2 = r["attenuation"]
+        m = mat.efficiency_measured
+        eff = np.interp(r["wavelength"], np.asarray(m.inputs.wavelength, dtype=np.float64),
+                        np.asarray(m.outputs, dtype=np.float64).reshape(-1))
     elif mirror:
         n2 = n1
         att2 = r["attenuation"]
     else:
         raise NotImplementedError(name)
     if rulings is not None:
-        eff = eff * getattr(rulings, "efficiency", 1.0)
+        eff = eff * ruling_efficiency(rulings, r, nx, ny, nz)
     rr = n1 / n2
     r["wavelength"] = r["wavelength"] / rr
     r["dx"], r["dy"], r["dz"] = snells_law(r["dx"], r["dy"], r["dz"], n1, n2, mirror, nx, ny, nz)

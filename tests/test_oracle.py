@@ -112,6 +112,8 @@ def _sags():
         ok.sags.ParabolicSag(focal_length=-150.0),
         ok.sags.ToroidalSag(radius=300.0, radius_of_rotation=500.0),
         ok.sags.ToroidalSag(radius=-400.0, radius_of_rotation=250.0),
+        ok.sags.CylindricalSag(radius=100.0),
+        ok.sags.CylindricalSag(radius=-100.0),
     ]
 
 
@@ -154,6 +156,30 @@ def test_normals_unit_with_negative_z(sag):
     nx, ny, nz = O.sag_normal(sag, x, y)
     assert np.allclose(nx**2 + ny**2 + nz**2, 1)
     assert np.all(nz < 0)
+
+
+def test_cylinder_known_answers():
+    """The cylinder is the sphere's x-z cross-section extruded along y
+    (optika/sags/_cylindrical.py:75-160): an axial ray at height x meets it
+    at R - sign(R) sqrt(R^2 - x^2), independent of y; a ray that misses the
+    cylinder stops at the vertex plane."""
+    for R in (80.0, -80.0):
+        sag = ok.sags.CylindricalSag(radius=R)
+        x = np.linspace(-30, 30, 13)
+        y = np.linspace(-50, 50, 13)
+        t = O.sag_intercept(sag, (x, y, np.full(13, -10.0)), (0 * x, 0 * x, np.ones(13)))
+        z = -10.0 + t
+        assert np.allclose(z, R - np.sign(R) * np.sqrt(R * R - x * x), atol=1e-12)
+        sph = ok.sags.SphericalSag(radius=R)
+        assert np.allclose(O.sag_value(sag, x, y), O.sag_value(sph, x, 0 * y), atol=1e-12)
+        nx, ny, nz = O.sag_normal(sag, x, y)
+        sx, sy, sz = O.sag_normal(sph, x, 0 * y)
+        assert np.allclose((nx, ny, nz), (sx, sy, sz), atol=1e-15)
+    # |x| > R: no real root, the vertex-plane intercept (o_z = -10, u_z = 1)
+    sag = ok.sags.CylindricalSag(radius=20.0)
+    t = O.sag_intercept(sag, (np.array([25.0]), np.array([3.0]), np.array([-10.0])),
+                        (np.array([0.0]), np.array([0.0]), np.array([1.0])))
+    assert np.allclose(t, 10.0)
 
 
 def test_parabola_equals_conic():

@@ -175,6 +175,10 @@ SURFACES = {
                                     material=ok.materials.Mirror()),
     "toroid": ok.surfaces.Surface(sag=ok.sags.ToroidalSag(600.0, 900.0),
                                   material=ok.materials.Mirror()),
+    "cylinder_mirror": ok.surfaces.Surface(sag=ok.sags.CylindricalSag(-400.0),
+                                           material=ok.materials.Mirror()),
+    "cylinder_lens": ok.surfaces.Surface(sag=ok.sags.CylindricalSag(250.0),
+                                         material=ok.materials.Glass.n_bk7()),
     "glass_lens": ok.surfaces.Surface(sag=ok.sags.SphericalSag(200.0),
                                       material=ok.materials.Glass.n_bk7()),
     "tilted_flat": ok.surfaces.Surface(
@@ -362,7 +366,7 @@ def test_sag_api(cuda):
     rng = np.random.default_rng(21)
     x, y = rng.uniform(-20, 20, (2, 1000))
     for sag in [ok.sags.SphericalSag(-200.0), ok.sags.ConicSag(300.0, -0.7),
-                ok.sags.ToroidalSag(400.0, 600.0)]:
+                ok.sags.ToroidalSag(400.0, 600.0), ok.sags.CylindricalSag(-150.0)]:
         z = sag(V3(x, y, 0.0)).cpu().numpy()
         assert np.allclose(z, O.sag_value(sag, x, y), atol=2e-6)
         n = sag.normal(V3(x, y, 0.0))
@@ -400,6 +404,17 @@ def test_edge_cases(cuda):
     out = _gpu_propagate([miss], r)
     ref = O.propagate_rays([miss], r)
     assert np.array_equal(np.isnan(out["px"]), np.isnan(ref["px"]))
+    # a cylinder the rays miss keeps them on its vertex plane, as in the
+    # reference (a sphere gives NaN instead)
+    cyl = ok.surfaces.Surface(sag=ok.sags.CylindricalSag(5.0), material=ok.materials.Mirror())
+    out = _gpu_propagate([cyl], r)
+    ref = O.propagate_rays([cyl], r)
+    assert np.array_equal(np.isnan(out["px"]), np.isnan(ref["px"]))
+    miss_ref = np.abs(ref["px"]) > 5.0
+    assert miss_ref.sum() > 50
+    ok_ = np.isfinite(ref["px"])
+    assert np.abs(out["px"][ok_] - ref["px"][ok_]).max() < 2e-4
+    assert np.abs(out["pz"][miss_ref] - ref["pz"][miss_ref]).max() < 1e-4
     # broadcast scalar wavelength and intensity
     g = configs.newtonian_grid(num_pupil=50)
     res = s.rayfunction(wavelength=550.0, field=V2(g["field_x"], g["field_y"]),
