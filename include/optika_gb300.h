@@ -105,11 +105,22 @@ typedef struct otx_affine {
  * `table` means the constant n_re + i n_im; otherwise the index of a
  * (wavelength, n, k) table in otx_system.tables, linearly interpolated and
  * clamped at the ends (optika/chemicals/_chemicals.py:138-142). */
+/* Interface profiles between layers (Stearns 1989), on the left side of a
+ * layer: the layer's reflection amplitude r_ij is multiplied by the Fourier
+ * transform of the profile's derivative (optika/materials/profiles.py). */
+#define OTX_PROFILE_NONE 0
+#define OTX_PROFILE_ERF 1         /* ErfInterfaceProfile, :130         */
+#define OTX_PROFILE_EXPONENTIAL 2 /* ExponentialInterfaceProfile, :226 */
+#define OTX_PROFILE_LINEAR 3      /* LinearInterfaceProfile, :328      */
+#define OTX_PROFILE_SINUSOIDAL 4  /* SinusoidalInterfaceProfile, :434  */
+
 typedef struct otx_layer {
   float n_re;
   float n_im;
   float thickness; /* nm */
   int32_t table;
+  int32_t interface_type; /* OTX_PROFILE_* of the interface on its left */
+  float interface_width;  /* nm */
 } otx_layer;
 
 /* A multilayer stack: `pre` layers, then `per` layers repeated

@@ -39,6 +39,7 @@ RULE_NONE, RULE_CONSTANT, RULE_POLY1D, RULE_HOLOGRAPHIC = range(4)
 INPUT_RAYS, INPUT_GRID_INFINITY, INPUT_GRID_FINITE = range(3)
 EPI_SILU_BF16, EPI_BIAS_F32, EPI_F32, EPI_DSILU_BF16, EPI_F32_ATOMIC = range(5)
 SYS_FLAG_FINAL_IDENTITY = 1
+PROFILE_NONE, PROFILE_ERF, PROFILE_EXPONENTIAL, PROFILE_LINEAR, PROFILE_SINUSOIDAL = range(5)
 
 f32 = ctypes.c_float
 i32 = ctypes.c_int32
@@ -61,7 +62,8 @@ class Affine(ctypes.Structure):
 
 
 class Layer(ctypes.Structure):
-    _fields_ = [("n_re", f32), ("n_im", f32), ("thickness", f32), ("table", i32)]
+    _fields_ = [("n_re", f32), ("n_im", f32), ("thickness", f32), ("table", i32),
+                ("interface_type", i32), ("interface_width", f32)]
 
 
 class Stack(ctypes.Structure):

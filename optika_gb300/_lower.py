@@ -19,6 +19,7 @@ import numpy as np
 from . import _lib as L
 from . import apertures as ap
 from . import materials as mt
+from . import profiles as pr
 from . import rulings as ru
 from . import sags as sg
 from .chemicals import Chemical
@@ -101,11 +102,18 @@ class Lowering:
     def _add_layer(self, layer: mt.Layer, substrate: bool = False) -> int:
         if self.n_layers >= L.MAX_LAYERS:
             raise ValueError(f"more than {L.MAX_LAYERS} layers in one system")
-        if getattr(layer, "interface", None) is not None:
-            raise NotImplementedError("interface roughness profiles are not supported on the GPU path")
         k = self.n_layers
         self.n_layers += 1
         lay = self.sys.layers[k]
+        iface = getattr(layer, "interface", None)
+        lay.interface_type = L.PROFILE_NONE
+        lay.interface_width = 0.0
+        if iface is not None:
+            if not isinstance(iface, pr.AbstractInterfaceProfile) or not 1 <= iface.tag <= 4:
+                raise NotImplementedError(
+                    f"interface profile {type(iface).__name__} is not supported on the GPU path")
+            lay.interface_type = iface.tag
+            lay.interface_width = float(iface.width)
         self._index_source(lay, layer.chemical)
         th = 0.0 if substrate or layer.thickness is None else float(layer.thickness)
         lay.thickness = th

@@ -73,6 +73,7 @@ struct MLff {
   ff t;
   int te;
   cff q;
+  cf n;  // index of the current medium (interface-profile factors)
   cff inv0;
   bool where;
 };
@@ -106,11 +107,21 @@ __device__ __forceinline__ void ff_normalize_scalar(ff& t, int& te) {
   te += e;
 }
 
+// An interface profile on the layer's left side scales r_ij, the
+// off-diagonal q_i - q_j (see layer_step in trace_device.cuh); its factor is
+// real, near 1 and evaluated in single precision.
 template <bool NEED_T>
 __device__ __forceinline__ void layer_step_ff(MLff& st, cf nj, float thickness, float wl,
-                                              bool pol_p) {
+                                              bool pol_p, int iface = OTX_PROFILE_NONE,
+                                              float iface_width = 0.f) {
   const cff qj = medium_q_ff(st.inv0, nj, pol_p);
-  const cff a = cff_add(st.q, qj), b = cff_sub(st.q, qj);
+  const cff a = cff_add(st.q, qj);
+  cff b = cff_sub(st.q, qj);
+  if (iface != OTX_PROFILE_NONE) {
+    const cf qi{st.q.re.hi, st.q.im.hi};
+    b = cff_scale(b, ff_of(interface_factor(iface, iface_width,
+                                            interface_wavenumber(qi, st.n, wl, pol_p))));
+  }
   bool wprop = true;
   cmff tm{a, b, b, a};
   if (thickness != 0.f) {
@@ -142,6 +153,7 @@ __device__ __forceinline__ void layer_step_ff(MLff& st, cf nj, float thickness, 
   }
   st.where = st.where && wprop;
   st.q = qj;
+  st.n = nj;
 }
 
 __device__ __forceinline__ void cmff_pow(cmff base, int bexp, int e, cmff& acc, int& aexp) {
@@ -186,6 +198,16 @@ struct SysStackSource {
   __device__ cf n_sub(float wl) const {
     return K.substrate >= 0 ? layer_n(sys, sys.layers[K.substrate], wl) : cf{1.f, 0.f};
   }
+  __device__ int iface(int section, int i) const { return lay(section, i).interface_type; }
+  __device__ float iface_width(int section, int i) const {
+    return lay(section, i).interface_width;
+  }
+  __device__ int sub_iface() const {
+    return K.substrate >= 0 ? sys.layers[K.substrate].interface_type : OTX_PROFILE_NONE;
+  }
+  __device__ float sub_iface_width() const {
+    return K.substrate >= 0 ? sys.layers[K.substrate].interface_width : 0.f;
+  }
 };
 
 struct PeriodicSource {
@@ -197,13 +219,19 @@ struct PeriodicSource {
   }
   __device__ float h(int, int i) const { return i == 0 ? P.thickness_a : P.thickness_b; }
   __device__ cf n_sub(float) const { return cf{P.n_sub_re, P.n_sub_im}; }
+  __device__ int iface(int, int) const { return OTX_PROFILE_NONE; }
+  __device__ float iface_width(int, int) const { return 0.f; }
+  __device__ int sub_iface() const { return OTX_PROFILE_NONE; }
+  __device__ float sub_iface_width() const { return 0.f; }
 };
 
 template <bool NEED_T, class S>
 __device__ __forceinline__ void run_section_ff(MLff& st, const S& src, int section, float wl,
                                                bool pol_p) {
   const int n = src.count(section);
-  for (int i = 0; i < n; ++i) layer_step_ff<NEED_T>(st, src.n(section, i, wl), src.h(section, i), wl, pol_p);
+  for (int i = 0; i < n; ++i)
+    layer_step_ff<NEED_T>(st, src.n(section, i, wl), src.h(section, i), wl, pol_p,
+                          src.iface(section, i), src.iface_width(section, i));
 }
 
 // Reflectivity and transmissivity of one polarisation (float-float), the
@@ -224,6 +252,7 @@ __device__ __forceinline__ void multilayer_pol_ff(const S& src, float wl, float 
     st.q = cff_scale(cff_conj(n0c), ff_div(ff_of(cos0), cff_abs2(n0c)));
   else
     st.q = cff_scale(n0c, ff_of(cos0));
+  st.n = n0;
   const cff q0 = st.q;
   st.where = true;
   run_section_ff<NEED_T>(st, src, 0, wl, pol_p);
@@ -251,9 +280,11 @@ __device__ __forceinline__ void multilayer_pol_ff(const S& src, float wl, float 
     }
     st.where = per.where;
     st.q = per.q;
+    st.n = per.n;
   }
   run_section_ff<NEED_T>(st, src, 2, wl, pol_p);
-  layer_step_ff<NEED_T>(st, src.n_sub(wl), 0.f, wl, pol_p);
+  layer_step_ff<NEED_T>(st, src.n_sub(wl), 0.f, wl, pol_p, src.sub_iface(),
+                        src.sub_iface_width());
   const ff m11 = cff_abs2(st.m.a);
   R = ff_to_f(ff_div(cff_abs2(st.m.c), m11));
   T = 0.f;
@@ -348,6 +379,7 @@ __device__ __forceinline__ void bilayer_pol_ff(const cff& q0, const cff& qa, con
   st.t = ff_of(1.f);
   st.te = 0;
   st.q = q0;
+  st.n = cf{1.f, 0.f};  // unused: the bilayer form has no interface profiles
   st.where = true;
   if (periods > 0) {
     bilayer_step(st, qa, &A);  // first period
@@ -374,6 +406,7 @@ __device__ __forceinline__ void bilayer_pol_ff(const cff& q0, const cff& qa, con
     }
     st.where = per.where;
     st.q = per.q;
+    st.n = per.n;
   }
   bilayer_step(st, qs, nullptr);  // into the substrate
   const ff m11 = cff_abs2(st.m.a);

@@ -116,9 +116,7 @@ static otx_status launch_trace(const otx_system* sys_in, int mode, const TraceAr
   for (int i = 0; i < sys->num_surfaces; ++i) {
     const otx_surface& s = sys->surfaces[i];
     if (s.mat_type == OTX_MAT_MULTILAYER_MIRROR || s.mat_type == OTX_MAT_MULTILAYER_FILM) {
-      const otx_stack& K = sys->stacks[s.mat_stack];
-      if (K.pre_count > 0 || (K.per_count > 0 && K.num_periods > 0) || K.post_count > 0)
-        ml = true;
+      if (stack_needs_product(*sys, sys->stacks[s.mat_stack])) ml = true;
     }
   }
   if (!(launch && launch->generic_only) && launch_fixed(mode, acc, rpt, grid, block, *sys, a, st))

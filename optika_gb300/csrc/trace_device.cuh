@@ -15,6 +15,7 @@
 #include <stdint.h>
 
 #include "../../include/optika_gb300.h"
+#include "trace_kernel_decl.h"
 
 namespace otx {
 
@@ -929,6 +930,38 @@ __device__ __forceinline__ cf layer_n(const otx_system& sys, const otx_layer& L,
   return cf{fmaf(w, ns[hi] - ns[lo], ns[lo]), fmaf(w, ks[hi] - ks[lo], ks[lo])};
 }
 
+// Fourier transform of the derivative of an interface profile at the
+// wavenumber s (1/nm), the factor on r_ij (Stearns 1989):
+//   erf          exp(-(s w)^2 / 2)             optika/materials/profiles.py:221-223
+//   exponential  1 / (1 + (s w)^2 / 2)                                    :320-326
+//   linear       sin(x) / x, x = sqrt(3) w s                              :424-431
+//   sinusoidal   pi (sin(x - pi/2) / (x - pi/2) + sin(x + pi/2) / (x + pi/2)) / 4,
+//                x = a w s, a = pi / (pi^2 - 8)                          :532-541
+__device__ __forceinline__ float interface_factor(int type, float width, float s) {
+  switch (type) {
+    case OTX_PROFILE_ERF: {
+      const float x = s * width;
+      return expf(-0.5f * x * x);
+    }
+    case OTX_PROFILE_EXPONENTIAL: {
+      const float x = s * width;
+      return 1.f / fmaf(0.5f * x, x, 1.f);
+    }
+    case OTX_PROFILE_LINEAR: {
+      const float x = 1.7320508075688772f * width * s;
+      return sinf(x) / x;
+    }
+    case OTX_PROFILE_SINUSOIDAL: {
+      const float pi = 3.14159265358979f;
+      const float x = (pi / (pi * pi - 8.f)) * width * s;
+      const float x1 = x - 0.5f * pi, x2 = x + 0.5f * pi;
+      return 0.25f * pi * (sinf(x1) / x1 + sinf(x2) / x2);
+    }
+    default:
+      return 1.f;
+  }
+}
+
 // Running state of the transfer-matrix product for one polarisation.
 //
 // The reference's refraction matrix W = [[1, r], [r, 1]] / t
@@ -946,6 +979,7 @@ struct MLState {
   float t;    // prod |2 q_i|^2 mantissa
   int te;     // and its exponent
   cf q;       // q of the current medium
+  cf n;       // index of the current medium
   cf inv0;    // (n0 sin0)^2, Snell invariant
   bool where;
 };
@@ -973,13 +1007,30 @@ __device__ __forceinline__ void ml_times(MLState& st, const cm2& t, int te) {
   cm_normalize(st.m, st.e);
 }
 
+// Wavenumber of an interface profile's factor from the incident medium
+// (optika/materials/profiles.py:103-128): s = Re(4 pi n_i d_i / lambda) with
+// d_i = cos_i for s and conj(cos_i) for p, i.e. 4 pi Re(q) / lambda for s
+// and 4 pi Re(q n_i^2) / lambda for p (q = conj(n cos) / |n|^2).
+__device__ __forceinline__ float interface_wavenumber(const cf& q, const cf& n, float wl,
+                                                      bool pol_p) {
+  const float re = pol_p ? cmul(q, cmul(n, n)).re : q.re;
+  return 12.566370614359172f * re / wl;
+}
+
 // Multiply the running product by one layer's W' (and its propagation U),
-// optika/materials/_layers.py:229-277; thickness 0 is the substrate.
+// optika/materials/_layers.py:229-277; thickness 0 is the substrate.  An
+// interface profile on the layer's left side scales r_ij, i.e. the
+// off-diagonal q_i - q_j of W' (optika/materials/matrices.py:147-152).
 template <bool NEED_T>
 __device__ __forceinline__ void layer_step(MLState& st, cf nj, float thickness, float wl,
-                                           bool pol_p) {
+                                           bool pol_p, int iface = OTX_PROFILE_NONE,
+                                           float iface_width = 0.f) {
   const cf qj = medium_q(st.inv0, nj, pol_p);
-  const cf a = cadd(st.q, qj), b = csub(st.q, qj);
+  const cf a = cadd(st.q, qj);
+  cf b = csub(st.q, qj);
+  if (iface != OTX_PROFILE_NONE)
+    b = cscale(b, interface_factor(iface, iface_width,
+                                   interface_wavenumber(st.q, st.n, wl, pol_p)));
   // U = diag(exp(-i beta), exp(i beta)), beta = 2 pi h n cos / lambda
   bool wprop = true;
   cm2 tm = cm2{a, b, b, a};
@@ -1007,6 +1058,7 @@ __device__ __forceinline__ void layer_step(MLState& st, cf nj, float thickness, 
   }
   st.where = st.where && wprop;
   st.q = qj;
+  st.n = nj;
 }
 
 __device__ __forceinline__ void cm_pow(cm2 base, int bexp, int e, cm2& acc, int& aexp) {
@@ -1037,7 +1089,8 @@ __device__ __forceinline__ void run_layers(MLState& st, const otx_system& sys, i
                                            int count, float wl, bool pol_p) {
   for (int i = 0; i < count; ++i) {
     const otx_layer& L = sys.layers[begin + i];
-    layer_step<NEED_T>(st, layer_n(sys, L, wl), L.thickness, wl, pol_p);
+    layer_step<NEED_T>(st, layer_n(sys, L, wl), L.thickness, wl, pol_p, L.interface_type,
+                       L.interface_width);
   }
 }
 
@@ -1057,6 +1110,7 @@ __device__ __forceinline__ void multilayer_pol(const otx_system& sys, const otx_
   st.te = 0;
   st.inv0 = cscale(cmul(n0, n0), fmaf(-cos0, cos0, 1.f));
   st.q = pol_p ? cscale(cconj(n0), cos0 / cabs2(n0)) : cscale(n0, cos0);
+  st.n = n0;
   const cf q0 = st.q;
   st.where = true;
   run_layers<NEED_T>(st, sys, K.pre_begin, K.pre_count, wl, pol_p);
@@ -1086,11 +1140,19 @@ __device__ __forceinline__ void multilayer_pol(const otx_system& sys, const otx_
     }
     st.where = per.where;
     st.q = per.q;
+    st.n = per.n;
   }
   run_layers<NEED_T>(st, sys, K.post_begin, K.post_count, wl, pol_p);
   cf nsub{1.f, 0.f};
-  if (K.substrate >= 0) nsub = layer_n(sys, sys.layers[K.substrate], wl);
-  layer_step<NEED_T>(st, nsub, 0.f, wl, pol_p);
+  int sub_iface = OTX_PROFILE_NONE;
+  float sub_width = 0.f;
+  if (K.substrate >= 0) {
+    const otx_layer& L = sys.layers[K.substrate];
+    nsub = layer_n(sys, L, wl);
+    sub_iface = L.interface_type;
+    sub_width = L.interface_width;
+  }
+  layer_step<NEED_T>(st, nsub, 0.f, wl, pol_p, sub_iface, sub_width);
   // R = |M21|^2 / |M11|^2 (exponents cancel)
   const float m11 = cabs2(st.m.a);
   R = cabs2(st.m.c) / m11;
@@ -1113,8 +1175,8 @@ __device__ __forceinline__ bool stack_has_layers(const otx_stack& K) {
   return K.pre_count > 0 || (K.per_count > 0 && K.num_periods > 0) || K.post_count > 0;
 }
 
-// Substrate-only stack (a bare coating, or a film of no layers): the
-// multilayer product reduces to one interface, r = (q0 - q1) / (q0 + q1),
+// Substrate-only stack with a smooth substrate (a bare coating, or a film of
+// no layers): the multilayer product reduces to one interface, r = (q0 - q1) / (q0 + q1),
 // t = 2 q0 / (q0 + q1); returns the s/p average of R (mirror) or T.
 __device__ __forceinline__ float fresnel_efficiency(const otx_system& sys, const otx_stack& K,
                                                     bool mirror, float wl, float cos0, cf n0) {
@@ -1246,7 +1308,7 @@ __device__ __forceinline__ void propagate_surface(const otx_system& sys,
       const float cos0 = -(r.dx * nx + r.dy * ny + r.dz * nz);
       const int ks = min(max(s.mat_stack, 0), OTX_MAX_STACKS - 1);
       const otx_stack& K2 = sys.stacks[ks];
-      if (mat_type != OTX_MAT_FRESNEL_MIRROR && ML && stack_has_layers(K2))
+      if (mat_type != OTX_MAT_FRESNEL_MIRROR && ML && stack_needs_product(sys, K2))
         eff = multilayer_efficiency_call(sys, ks, mirror, r.wl, cos0, n1, k);
       else
         eff = fresnel_efficiency(sys, K2, mirror, r.wl, cos0, cf{n1, k});

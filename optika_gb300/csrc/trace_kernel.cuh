@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
 inline int effective_mat(const otx_system& sys, const otx_surface& s) {
   if (s.mat_type == OTX_MAT_MULTILAYER_MIRROR) {
     const otx_stack& K = sys.stacks[s.mat_stack];
-    if (!(K.pre_count > 0 || (K.per_count > 0 && K.num_periods > 0) || K.post_count > 0))
+    if (!stack_needs_product(sys, K))
       return OTX_MAT_FRESNEL_MIRROR;
   }
   return s.mat_type;

@@ -14,6 +14,16 @@ __host__ __device__ __forceinline__ bool image_any(const otx_image& img) {
   return img.counts != 0 || img.flux != 0 || img.cos_moment != 0;
 }
 
+// Whether a multilayer stack needs the transfer-matrix product: layers, or
+// a rough substrate.  A smooth bare substrate takes the Fresnel form, which
+// has no interface profile and keeps the shape-specialised kernels small.
+__host__ __device__ __forceinline__ bool stack_needs_product(const otx_system& sys,
+                                                             const otx_stack& K) {
+  return K.pre_count > 0 || (K.per_count > 0 && K.num_periods > 0) || K.post_count > 0 ||
+         (K.substrate >= 0 && K.substrate < OTX_MAX_LAYERS &&
+          sys.layers[K.substrate].interface_type != OTX_PROFILE_NONE);
+}
+
 // Checks of a system descriptor shared by every entry point that traces
 // through it: type tags, pool indices and sizes (OTX_OK when usable).
 otx_status validate_system(const otx_system* sys);

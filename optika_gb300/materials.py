@@ -15,6 +15,7 @@ from __future__ import annotations
 import dataclasses
 from typing import Sequence, Union
 
+from . import profiles  # noqa: F401  (optika.materials.profiles)
 from .chemicals import Chemical
 from .vectors import PolarizationVectorArray
 

@@ -451,7 +451,34 @@ def layer_index(chemical, wavelength):
     return np.full(w.shape, complex(chemical))
 
 
-def _refraction(cos_i, cos_j, n_i, n_j, s):
+def interface_reflectivity(interface, wavelength, direction, n):
+    """Factor of an interface profile on r_ij: the Fourier transform of the
+    profile's derivative at s = Re(-2 k), k = -2 pi n direction / lambda
+    (optika/materials/profiles.py:103-128; transforms :221-223 erf,
+    :320-326 exponential, :424-431 linear, :532-541 sinusoidal)."""
+    if interface is None:
+        return 1.0
+    w = interface.width
+    k = -2 * np.pi * n * direction / wavelength
+    sv = np.real(-2 * k)
+    name = type(interface).__name__
+    with np.errstate(all="ignore"):
+        if name == "ErfInterfaceProfile":
+            return np.exp(-np.square(sv * w) / 2)
+        if name == "ExponentialInterfaceProfile":
+            return 1 / (1 + np.square(sv * w) / 2)
+        if name == "LinearInterfaceProfile":
+            x = np.sqrt(3) * w * sv
+            return np.sin(x) / x
+        if name == "SinusoidalInterfaceProfile":
+            a = np.pi / (np.square(np.pi) - 8)
+            x = a * w * sv
+            x1, x2 = x - np.pi / 2, x + np.pi / 2
+            return np.pi * (np.sin(x1) / x1 + np.sin(x2) / x2) / 4
+    raise NotImplementedError(name)
+
+
+def _refraction(cos_i, cos_j, n_i, n_j, s, wavelength=None, interface=None):
     """optika/materials/matrices.py:127-161 for one polarisation."""
     ci = cos_i if s else np.conj(cos_i)
     cj = cos_j if s else np.conj(cos_j)
@@ -460,6 +487,8 @@ def _refraction(cos_i, cos_j, n_i, n_j, s):
     a = qi + qj
     r = (qi - qj) / a
     t = 2 * qi / a
+    if interface is not None:
+        r = r * interface_reflectivity(interface, wavelength, ci, n_i)
     one = np.ones_like(r)
     return np.stack([np.stack([one, r], -1), np.stack([r, one], -1)], -2) / t[..., None, None]
 
@@ -473,11 +502,11 @@ def _propagation(wavelength, cos, thickness, n):
     )
 
 
-def _layer_transfer(layer_chem, thickness, wavelength, cos, n, s, where):
+def _layer_transfer(layer_chem, thickness, wavelength, cos, n, s, where, interface=None):
     """optika/materials/_layers.py:229-277."""
     n_int = layer_index(layer_chem, wavelength)
     cos_int = snells_law_scalar(cos, n, n_int)
-    W = _refraction(cos, cos_int, n, n_int, s)
+    W = _refraction(cos, cos_int, n, n_int, s, wavelength, interface)
     eye = np.broadcast_to(np.eye(2, dtype=complex), W.shape)
     W = np.where(where[..., None, None], W, eye)
     with np.errstate(all="ignore"):
@@ -514,7 +543,8 @@ def _sequence_transfer(items, wavelength, cos, n, s, where):
             P = np.linalg.matrix_power(per, int(it.num_periods) - 1)
             M = M @ start @ P
         else:
-            n, cos, T, where = _layer_transfer(it.chemical, it.thickness, wavelength, cos, n, s, where)
+            n, cos, T, where = _layer_transfer(it.chemical, it.thickness, wavelength, cos, n, s,
+                                               where, getattr(it, "interface", None))
             M = M @ T
     return n, cos, M, where
 
@@ -533,7 +563,8 @@ def multilayer_efficiency(wavelength, direction=1.0, n=1.0, layers=None, substra
     for s in (True, False):
         where = np.ones(wavelength.shape, dtype=bool)
         n1, c1, M, where = _sequence_transfer(items, wavelength, direction, n, s, where)
-        n1, c1, Ms, where = _layer_transfer(sub_chem, 0.0, wavelength, c1, n1, s, where)
+        n1, c1, Ms, where = _layer_transfer(sub_chem, 0.0, wavelength, c1, n1, s, where,
+                                            getattr(substrate, "interface", None))
         M = M @ Ms
         r = M[..., 1, 0] / M[..., 0, 0]
         t = 1 / M[..., 0, 0]

@@ -29,8 +29,11 @@ def golden_case(name):
     th = z[f"{name}/thickness"]
     nc = int(z[f"{name}/num_chemicals"])
     chems = [ok.chemicals.Chemical(wl, z[f"{name}/n{i}"], z[f"{name}/k{i}"]) for i in range(nc)]
-    layers = [ok.materials.Layer(chems[i], th[i]) for i in range(len(th))]
-    sub = ok.materials.Layer(chems[-1])
+    sigma = float(z[f"{name}/interface_width"])
+    prof = (lambda: ok.materials.profiles.ErfInterfaceProfile(sigma)) if sigma > 0 else (
+        lambda: None)
+    layers = [ok.materials.Layer(chems[i], th[i], interface=prof()) for i in range(len(th))]
+    sub = ok.materials.Layer(chems[-1], interface=prof())
     return wl, z[f"{name}/efficiency"], bool(z[f"{name}/is_mirror"]), layers, sub
 
 
