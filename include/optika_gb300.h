@@ -558,6 +558,46 @@ otx_status otx_collect(const otx_sensor* sensor, const otx_rays* rays,
 otx_status otx_sag_eval(const otx_system* sys, int32_t mode, const otx_rays* in,
                         const otx_rays* out, void* stream);
 
+/* Cells of a scene for SequentialSystem.image (optika/systems/
+ * _sequential.py:1002-1086 _rayfunction_from_vertices): one ray per cell
+ * of the (wavelength, field x, field y, pupil x, pupil y) vertex grid, at a
+ * uniformly drawn point of the cell (or its centre), carrying the cell's
+ * flux.  Field and pupil vertices are given at every wavelength vertex
+ * (normalised coordinates are denormalised per wavelength by the stop
+ * solver); inside a cell they are interpolated with the same wavelength
+ * weight as the wavelength itself.  All tables are float device arrays. */
+typedef struct otx_cells {
+  uint64_t wavelength;   /* [nw + 1] vertices (nm)                          */
+  uint64_t field_x;      /* [nw + 1][nfx + 1]                                */
+  uint64_t field_y;      /* [nw + 1][nfy + 1]                                */
+  uint64_t pupil_x;      /* [nw + 1][npx + 1]                                */
+  uint64_t pupil_y;      /* [nw + 1][npy + 1]                                */
+  uint64_t weight;       /* [nw][nfx][nfy] radiance x wavelength width x
+                            field cell area (solid angle or area)            */
+  uint64_t weight_pupil; /* [nw][npx][npy] pupil cell area (or solid angle) */
+  int32_t nw, nfx, nfy, npx, npy;
+  int32_t random;        /* 1: uniform point of each cell; 0: its centre     */
+  uint64_t seed;         /* Philox key of the draws                          */
+} otx_cells;
+
+/* Input rays of cells [first, first + count) (ray index = ((((iw nfx + ifx)
+ * nfy + ify) npx + ipx) npy + ipy) into out->wavelength, field_x, field_y,
+ * pupil_x, pupil_y and intensity (each a float array of `count` entries;
+ * out's strides are ignored).  The rays then go through otx_trace_grid
+ * with sensor binning, as rayfunction does in the reference. */
+otx_status otx_cell_rays(const otx_cells* cells, int64_t first, int64_t count,
+                         const otx_grid* out, void* stream);
+
+/* Detector exposure of an ideal sensor (optika/sensors/_sensors.py:173-252
+ * expose; optika/sensors/materials/_materials.py:1576-1598 signal):
+ * electrons[i] = Poisson(scale photons[i]) + read_noise N(0, 1) when
+ * `noise` is set, scale photons[i] otherwise.  Poisson variates by
+ * transformed rejection (Hormann 1993) for means >= 10 and by the
+ * multiplication method below; normal variates by Box-Muller; one Philox
+ * stream per pixel keyed by `seed`. */
+otx_status otx_expose(const float* photons, float* electrons, int64_t count, float scale,
+                      float read_noise, int32_t noise, uint64_t seed, void* stream);
+
 /* Evaluate the rulings of sys->surfaces[0] for rays at the surface (in the
  * surface frame) with the sag normals `normal` (normal->dx, dy, dz; the
  * rays' direction in rays->d*, position in rays->p*, wavelength in nm).

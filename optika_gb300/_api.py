@@ -143,7 +143,7 @@ class PreparedTrace:
 
     def __init__(self, system, *, wavelength, field, pupil, intensity=None, accumulate=False,
                  final_local=True, image=False, wavelength_bins=None, launch=None,
-                 outputs=OUTPUT_FIELDS):
+                 outputs=OUTPUT_FIELDS, cos_moment=False):
         dev = device()
         self.device = dev
         surfaces = system.surfaces_all
@@ -193,17 +193,24 @@ class PreparedTrace:
         self.bufs = _alloc_rays(n, dev, (self.num_surfaces,) if accumulate else (), outputs)
         self.out = _rays_struct(self.bufs, n, n if accumulate else 0)
         self.img = L.Image()
-        self.counts = self.flux = None
+        self.counts = self.flux = self.moment = None
         if image:
-            self.counts, self.flux, self.img = _image_buffers(sensor, wavelength_bins, dev)
+            bufs = _image_buffers(sensor, wavelength_bins, dev, cos_moment=cos_moment)
+            self.counts, self.flux, self.img = bufs[:3]
+            if cos_moment:
+                self.moment = bufs[3]
         self.launch_desc = launch if launch is not None else L.Launch()
         self.launch_desc.accumulate = 1 if accumulate else 0
         self.lib = L.load()
 
-    def run(self) -> None:
-        if self.counts is not None:
+    def run(self, clear: bool = True) -> None:
+        """One trace launch; ``clear=False`` adds to the images of earlier
+        runs instead of starting from zero."""
+        if self.counts is not None and clear:
             self.counts.zero_()
             self.flux.zero_()
+            if self.moment is not None:
+                self.moment.zero_()
         st = self.lib.otx_trace_grid(
             ctypes.byref(self.lowering.sys), ctypes.byref(self.grid), ctypes.byref(self.out),
             ctypes.byref(self.img), ctypes.byref(self.launch_desc), stream_handle(),
@@ -572,3 +579,21 @@ def multilayer_periodic_gpu(wavelength, direction, mirrors, index, n):
     L.check(st, "otx_multilayer_periodic")
     rs, rp, ts, tp = (o.reshape(shape) for o in outs)
     return PolarizationVectorArray(rs, rp), PolarizationVectorArray(ts, tp)
+
+
+def cell_rays(cells: L.Cells, first: int, count: int, grid: L.Grid) -> None:
+    """Input rays of scene cells [first, first + count) into the grid's
+    arrays (otx_cell_rays)."""
+    L.check(L.load().otx_cell_rays(ctypes.byref(cells), first, count, ctypes.byref(grid),
+                                   stream_handle()), "otx_cell_rays")
+
+
+def expose(photons: torch.Tensor, scale: float, read_noise: float, noise: bool,
+           seed: int) -> torch.Tensor:
+    """Electrons of an ideal sensor (otx_expose) from a photon image."""
+    p = photons.to(device=device(), dtype=torch.float32).contiguous()
+    out = torch.empty_like(p)
+    L.check(L.load().otx_expose(ptr(p), ptr(out), p.numel(), float(scale), float(read_noise),
+                                1 if noise else 0, int(seed) & (2**64 - 1), stream_handle()),
+            "otx_expose")
+    return out

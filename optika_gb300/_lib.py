@@ -283,6 +283,25 @@ class Launch(ctypes.Structure):
     ]
 
 
+class Cells(ctypes.Structure):
+    _fields_ = [
+        ("wavelength", u64),
+        ("field_x", u64),
+        ("field_y", u64),
+        ("pupil_x", u64),
+        ("pupil_y", u64),
+        ("weight", u64),
+        ("weight_pupil", u64),
+        ("nw", i32),
+        ("nfx", i32),
+        ("nfy", i32),
+        ("npx", i32),
+        ("npy", i32),
+        ("random", i32),
+        ("seed", u64),
+    ]
+
+
 LAYOUT = {
     0: System,
     1: Surface,
@@ -298,6 +317,7 @@ LAYOUT = {
     11: Batch,
     12: Surrogate,
     13: Mlp,
+    14: Cells,
 }
 
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "_lib" / "liboptika_gb300.so"
@@ -379,6 +399,10 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_sag_eval.restype = i32
     lib.otx_rulings_eval.argtypes = [P(System), i32, P(Rays), P(Rays), v, P(Rays), v]
     lib.otx_rulings_eval.restype = i32
+    lib.otx_cell_rays.argtypes = [P(Cells), i64, i64, P(Grid), v]
+    lib.otx_cell_rays.restype = i32
+    lib.otx_expose.argtypes = [v, v, i64, f32, f32, i32, u64, v]
+    lib.otx_expose.restype = i32
 
 
 def load() -> ctypes.CDLL:

@@ -470,6 +470,7 @@ int64_t otx_sizeof(int32_t which) {
     case 11: return sizeof(otx_batch);
     case 12: return sizeof(otx_surrogate);
     case 13: return sizeof(otx_mlp);
+    case 14: return sizeof(otx_cells);
     default: return -1;
   }
 }

@@ -91,3 +91,41 @@ class ImagingSensor(AbstractSurface):
         from ._api import collect
 
         return collect(self, rays, wavelength=wavelength, where=where)
+
+    def expose(self, image, direction=1, timedelta=None, noise: bool = True, seed: int = 0,
+               photons: bool = True, wavelength=None):
+        """Electrons measured from a photon image (optika/sensors/_sensors.py:
+        173-252 with the ideal material, optika/sensors/materials/
+        _materials.py:1576-1598), on the GPU: ``image x timedelta`` photons
+        per pixel, Poisson shot noise and Gaussian read noise of
+        ``read_noise`` electrons when ``noise``.  ``timedelta`` defaults to
+        ``timedelta_exposure``.  ``photons=False`` means the image is an
+        energy flux (J), converted to photons with h c / lambda at the
+        centres of the wavelength bin edges ``wavelength`` (nm).  The ideal
+        material's quantum efficiency is 1, so ``direction`` (the refracted
+        cosine) does not enter."""
+        import torch
+
+        from ._api import device, expose
+
+        img = image if isinstance(image, torch.Tensor) else torch.as_tensor(
+            np.asarray(image, dtype=np.float32))
+        img = img.to(device=device(), dtype=torch.float32)
+        if not photons:
+            if wavelength is None:
+                raise ValueError("an energy image needs the wavelength bin edges")
+            w = np.asarray(wavelength, dtype=np.float64)
+            centers = (w[:-1] + w[1:]) / 2
+            hc = 6.62607015e-34 * 299792458.0 * 1e9  # J nm
+            per = torch.as_tensor(centers / hc, dtype=torch.float32, device=img.device)
+            img = img * per.reshape((-1,) + (1,) * (img.ndim - 1))
+        dt = self.timedelta_exposure if timedelta is None else timedelta
+        return expose(img, float(dt), float(self.read_noise), noise, seed)
+
+    def measure(self, rays, wavelength=None, where=True, timedelta=None, noise: bool = True,
+                seed: int = 0):
+        """:meth:`collect` then :meth:`expose` (optika/sensors/_sensors.py:
+        374-428): electrons per pixel ``[num_w, num_x, num_y]``."""
+        image, direction = self.collect(rays, wavelength=wavelength, where=where)
+        return self.expose(image, direction=direction, timedelta=timedelta, noise=noise,
+                           seed=seed)

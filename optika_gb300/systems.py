@@ -197,3 +197,36 @@ class SequentialSystem:
         )
         res.inputs = ObjectVectorArray(wavelength=wl, field=fld, pupil=pup)
         return res
+
+    def image(
+        self,
+        scene,
+        pupil=None,
+        normalized_field: bool = True,
+        normalized_pupil: bool = True,
+        integrate: bool = True,
+        noise: bool = True,
+        random: bool = True,
+        seed: int = 0,
+        timedelta=None,
+        chunk: int = 1 << 24,
+    ):
+        """Forward model: detector electrons of a scene of spectral radiance
+        given on cell vertices (optika/systems/_sequential.py:1088-1206).
+
+        ``scene`` is a :class:`~optika_gb300.vectors.FunctionArray` whose
+        inputs are a :class:`~optika_gb300.vectors.SpectralPositionalVectorArray`
+        of wavelength vertices (nm) and field vertices (a
+        ``Cartesian2dVectorArray`` of 1-D x and y vertices) and whose outputs
+        are the radiance of each cell ``[nw, nfx, nfy]``; ``pupil`` holds
+        pupil vertices (default one normalised cell ``[-1, 1]^2``).  The
+        reference decides from units whether coordinates are normalised;
+        here ``normalized_field`` / ``normalized_pupil`` say so.  Returns a
+        ``FunctionArray`` of wavelength bin edges and pixel edges to
+        electrons ``[num_w, num_pixel_x, num_pixel_y]`` (one wavelength bin
+        when ``integrate``).  See :mod:`optika_gb300.imaging`."""
+        from .imaging import image
+
+        return image(self, scene, pupil=pupil, normalized_field=normalized_field,
+                     normalized_pupil=normalized_pupil, integrate=integrate, noise=noise,
+                     random=random, seed=seed, timedelta=timedelta, chunk=chunk)

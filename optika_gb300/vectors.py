@@ -21,6 +21,7 @@ __all__ = [
     "ObjectVectorArray",
     "PolarizationVectorArray",
     "SpectralDirectionalVectorArray",
+    "SpectralPositionalVectorArray",
     "FunctionArray",
     "spectral_table",
 ]
@@ -73,6 +74,14 @@ class SpectralDirectionalVectorArray:
 
     wavelength: Any = 550.0
     direction: Any = None
+
+
+@dataclasses.dataclass
+class SpectralPositionalVectorArray:
+    """A wavelength (nm) and a position (a Cartesian2dVectorArray)."""
+
+    wavelength: Any = 550.0
+    position: Any = None
 
 
 @dataclasses.dataclass
