@@ -598,6 +598,21 @@ otx_status otx_cell_rays(const otx_cells* cells, int64_t first, int64_t count,
 otx_status otx_expose(const float* photons, float* electrons, int64_t count, float scale,
                       float read_noise, int32_t noise, uint64_t seed, void* stream);
 
+/* Masked reductions of traced rays over the pupil, the first step of the
+ * reference's calibration fits (optika/systems/_sequential.py:1208-1512:
+ * distortion, vignetting, area_effective).  The rays are `groups` runs of
+ * `per_group` consecutive rays (one run per wavelength and field point,
+ * the pupil fastest).  For each group g, sums[g * 6 + k] receives
+ *   k = 0: the number of unvignetted rays,
+ *       1, 2: the sums of px, py over the unvignetted rays,
+ *       3, 4: the sums of px, py over all rays,
+ *       5: the sum of intensity over the unvignetted rays
+ * (double precision).  Reads px, py, intensity (1 if null) and
+ * unvignetted (all if null) of `rays`; rays->count must be
+ * groups * per_group. */
+otx_status otx_pupil_reduce(const otx_rays* rays, int64_t groups, int64_t per_group,
+                            double* sums, void* stream);
+
 /* Evaluate the rulings of sys->surfaces[0] for rays at the surface (in the
  * surface frame) with the sag normals `normal` (normal->dx, dy, dz; the
  * rays' direction in rays->d*, position in rays->p*, wavelength in nm).

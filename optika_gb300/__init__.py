@@ -12,7 +12,10 @@ import math
 from . import (
     apertures,
     chemicals,
+    distortion,
     materials,
+    profiles,
+    radiometry,
     rays,
     rulings,
     sags,
@@ -30,7 +33,10 @@ deg = math.pi / 180.0
 __all__ = [
     "apertures",
     "chemicals",
+    "distortion",
     "materials",
+    "profiles",
+    "radiometry",
     "rays",
     "rulings",
     "sags",

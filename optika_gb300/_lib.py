@@ -399,6 +399,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_sag_eval.restype = i32
     lib.otx_rulings_eval.argtypes = [P(System), i32, P(Rays), P(Rays), v, P(Rays), v]
     lib.otx_rulings_eval.restype = i32
+    lib.otx_pupil_reduce.argtypes = [P(Rays), i64, i64, v, v]
+    lib.otx_pupil_reduce.restype = i32
     lib.otx_cell_rays.argtypes = [P(Cells), i64, i64, P(Grid), v]
     lib.otx_cell_rays.restype = i32
     lib.otx_expose.argtypes = [v, v, i64, f32, f32, i32, u64, v]

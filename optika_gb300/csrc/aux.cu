@@ -116,6 +116,50 @@ __global__ void k_rulings(const __grid_constant__ otx_system sys, const int mode
   }
 }
 
+// One block per group (grid-stride over groups): per-thread double
+// partial sums, then a warp-shuffle and shared-memory tree.
+__global__ void __launch_bounds__(256) k_pupil_reduce(const otx_rays r, int64_t groups,
+                                                      int64_t per, double* sums) {
+  __shared__ double part[6][8];
+  const float* px = reinterpret_cast<const float*>(r.px);
+  const float* py = reinterpret_cast<const float*>(r.py);
+  const float* in = reinterpret_cast<const float*>(r.intensity);
+  const uint8_t* uv = reinterpret_cast<const uint8_t*>(r.unvignetted);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t g = blockIdx.x; g < groups; g += gridDim.x) {
+    double a[6] = {0, 0, 0, 0, 0, 0};
+    const int64_t base = g * per;
+    for (int64_t k = threadIdx.x; k < per; k += blockDim.x) {
+      const int64_t i = base + k;
+      const double x = px[i], y = py[i];
+      a[3] += x;
+      a[4] += y;
+      if (!uv || uv[i]) {
+        a[0] += 1.0;
+        a[1] += x;
+        a[2] += y;
+        a[5] += in ? (double)in[i] : 1.0;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a[j] += __shfl_down_sync(0xffffffffu, a[j], o);
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < 6; ++j) part[j][warp] = a[j];
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[threadIdx.x][w];
+      sums[g * 6 + threadIdx.x] = t;
+    }
+    __syncthreads();
+  }
+}
+
 static int grid_for(int64_t n) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -184,5 +228,22 @@ extern "C" otx_status otx_rulings_eval(const otx_system* sys, int32_t mode, cons
   const otx_rays none{};
   k_rulings<<<grid_for(rays->count), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
       *sys, mode, *rays, *normal, efficiency, mode == 1 ? *out : none);
+  return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
+}
+
+extern "C" otx_status otx_pupil_reduce(const otx_rays* rays, int64_t groups, int64_t per_group,
+                                       double* sums, void* stream) {
+  if (!rays || groups < 0 || per_group < 1) return OTX_ERR_INVALID;
+  if (groups == 0) return OTX_OK;
+  if (!rays->px || !rays->py || !sums) return OTX_ERR_INVALID;
+  if (rays->count != groups * per_group) return OTX_ERR_INVALID;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms <= 0) sms = 132;
+  const int64_t cap = (int64_t)sms * 8;
+  const int grid = (int)(groups < cap ? groups : cap);
+  k_pupil_reduce<<<grid, 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*rays, groups,
+                                                                           per_group, sums);
   return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
 }

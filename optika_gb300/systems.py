@@ -230,3 +230,32 @@ class SequentialSystem:
         return image(self, scene, pupil=pupil, normalized_field=normalized_field,
                      normalized_pupil=normalized_pupil, integrate=integrate, noise=noise,
                      random=random, seed=seed, timedelta=timedelta, chunk=chunk)
+
+    # ---- calibration fits (optika/systems/_sequential.py:1208-1512)
+
+    def distortion(self, wavelength=None, field=None, pupil=None, normalized_field: bool = True,
+                   normalized_pupil: bool = True, degree: int = 2):
+        """Polynomial distortion model fitted to traced rays; grids are 1-D
+        arrays per coordinate (see :mod:`optika_gb300.calibration`)."""
+        from .calibration import distortion
+
+        return distortion(self, wavelength, field, pupil, normalized_field, normalized_pupil,
+                          degree)
+
+    def vignetting(self, wavelength=None, field=None, pupil=None, normalized_field: bool = True,
+                   normalized_pupil: bool = True, degree: int = 2):
+        """Polynomial vignetting model fitted to traced rays."""
+        from .calibration import vignetting
+
+        return vignetting(self, wavelength, field, pupil, normalized_field, normalized_pupil,
+                          degree)
+
+    def area_effective(self, wavelength=None, field=None, pupil=None,
+                       normalized_field: bool = True, normalized_pupil: bool = True,
+                       random: bool = True, seed: int = 0):
+        """Effective area versus wavelength from traced rays (pupil given on
+        cell vertices)."""
+        from .calibration import area_effective
+
+        return area_effective(self, wavelength, field, pupil, normalized_field,
+                              normalized_pupil, random, seed)
