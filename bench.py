@@ -501,6 +501,130 @@ def run_multilayer(args, rank: int, world: int) -> None:
         }), flush=True)
 
 
+_IMAGE_SURFACES = 5  # object, obscuration, primary, fold, sensor
+
+
+def _image_scene(seed: int = 6):
+    """The forward-model workload: 8 wavelength cells over 400-700 nm,
+    128 x 128 field cells over +-0.15 deg of seeded radiance, 32 x 32 pupil
+    cells over +-50 mm: 1.34e8 cells (rays) per image."""
+    from optika_gb300.vectors import (Cartesian2dVectorArray, FunctionArray,
+                                      SpectralPositionalVectorArray)
+
+    rng = np.random.default_rng(seed)
+    w = np.linspace(400.0, 700.0, 9)
+    f = np.linspace(-0.15, 0.15, 129) * math.pi / 180
+    rad = rng.uniform(0.5, 1.5, (8, 128, 128))
+    v = np.linspace(-50.0, 50.0, 33)
+    scene = FunctionArray(inputs=SpectralPositionalVectorArray(
+        wavelength=w, position=Cartesian2dVectorArray(f, f)), outputs=rad)
+    return scene, Cartesian2dVectorArray(v, v)
+
+
+_IMAGE_TABLES = {}
+
+
+def _cpu_image_worker(args):
+    first, count, seed = args
+    from optika_gb300 import configs
+    from oracle import image as OI
+
+    if "t" not in _IMAGE_TABLES:
+        system = configs.newtonian(coated=True)
+        scene, pupil = _image_scene()
+        _IMAGE_TABLES["s"] = system
+        _IMAGE_TABLES["t"] = OI.cell_tables(system, scene.inputs.wavelength,
+                                            scene.inputs.position.x, scene.inputs.position.y,
+                                            scene.outputs, pupil.x, pupil.y, False, False)
+    inputs = OI.cell_inputs(_IMAGE_TABLES["t"], True, seed, first, count)
+    OI.photon_image(_IMAGE_TABLES["s"], inputs, (400.0, 700.0, 1))
+    return (count,)
+
+
+def run_image(args, rank: int, world: int) -> None:
+    """SequentialSystem.image of the Al-coated Newtonian: cell rays drawn on
+    the device, the fused trace with sensor binning, exposure with shot and
+    read noise, 1.34e8 cells per image in chunks of 2^24.  Replicas under
+    torchrun (each rank its own seed)."""
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from optika_gb300 import configs
+    from optika_gb300.imaging import ImagePlan
+
+    system = configs.newtonian(coated=True)
+    system.sensor.read_noise = 2.0
+    scene, pupil = _image_scene()
+    seed = 6 + 1000 * rank
+    plan = ImagePlan(system, scene, pupil, normalized_field=False, normalized_pupil=False,
+                     integrate=True, random=True, seed=seed)
+    n = plan.count
+
+    def step():
+        return plan.run(noise=True, timedelta=1.0)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    value = world * n * _IMAGE_SURFACES / (ms * 1e-3)
+    # end to end: the public call, host tables included, electrons to the host
+    e2e_ms = []
+    for _ in range(max(1, args.e2e_steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = system.image(scene, pupil=pupil, normalized_field=False, normalized_pupil=False,
+                           noise=True, seed=seed, timedelta=1.0)
+        host = res.outputs.cpu()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e = sorted(e2e_ms)[len(e2e_ms) // 2]
+    tables = sum(np.asarray(a).nbytes // 2 for a in (
+        plan.tables.wavelength, plan.tables.field_x, plan.tables.field_y, plan.tables.pupil_x,
+        plan.tables.pupil_y, plan.tables.weight, plan.tables.weight_pupil))  # float32 copies
+    bpr = 48  # cell rays: 24 B written; trace: the same 24 B read
+    pk, pk_kind = peaks()
+    ach = bpr * n / (ms * 1e-3) / 1e9
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores = len(os.sched_getaffinity(0))
+        per = 250_000
+        jobs = [(k * 7_919_993 % (n - per), per, seed) for k in range(cores)]
+        rays, wall = _cpu_pool(_cpu_image_worker, jobs, cores)
+        cpu = {"value": rays * _IMAGE_SURFACES / wall, "unit": "rays*surfaces/s",
+               "cores": cores, "kind": "port",
+               "sample": f"{len(jobs)} x {per} cells of the same image, float64 ({wall:.1f} s)"}
+    if rank == 0:
+        print(json.dumps({
+            "metric": "rays*surfaces/s (SequentialSystem.image forward model)",
+            "value": value, "unit": "rays*surfaces/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "newtonian-image (Al-coated)", "cells": n,
+                       "grid": "8 wavelengths x 128^2 field x 32^2 pupil", "surfaces": 5,
+                       "sensor": "1024x1024 x 13.5um", "chunk": plan.chunk,
+                       "l2": "per-chunk ray inputs 400 MB, larger than L2"},
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": ach / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+                         "bytes_per_ray": bpr, "kernel": "k_cell_rays + k_trace_fixed",
+                         "kernel_ms": ms,
+                         "note": "the trace is FP32-issue-bound: the byte roofline is shown "
+                                 "for completeness"},
+            "e2e": {"value": world * n * _IMAGE_SURFACES / (e2e * 1e-3), "unit": "rays*surfaces/s",
+                    "ms_per_step": e2e, "h2d_bytes_per_step": int(tables),
+                    "d2h_bytes_per_step": int(host.numel() * host.element_size())},
+            "cpu_baseline": cpu, "gpu_launches": plan.launches * args.steps, "clocks": clk,
+        }), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -514,7 +638,7 @@ def main() -> None:
                     help="rays per step of the reference (CPU) arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="precision",
-                    choices=["precision", "surrogate", "batched", "multilayer"])
+                    choices=["precision", "surrogate", "batched", "multilayer", "image"])
     ap.add_argument("--configs", type=int, default=4096, help="batched workload configurations")
     ap.add_argument("--samples", type=int, default=10_000_000,
                     help="multilayer workload samples per step")
@@ -542,6 +666,9 @@ def main() -> None:
         return
     if args.workload == "multilayer":
         run_multilayer(args, rank, world)
+        return
+    if args.workload == "image":
+        run_image(args, rank, world)
         return
 
     import torch

@@ -21,33 +21,36 @@ __device__ __forceinline__ float cell_lerp(const float* t, int n, int iw, int k,
   return fmaf(hi - lo, uw, lo);
 }
 
+// IDX is the type of the cell-index arithmetic: 32-bit when every index
+// of the scene fits (the divisions are then a fraction of the 64-bit ones).
+template <typename IDX>
 __global__ void __launch_bounds__(256) k_cell_rays(const otx_cells c, int64_t first,
                                                    int64_t count, otx_grid out) {
   const int64_t step = (int64_t)gridDim.x * blockDim.x;
   const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
   for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += step) {
     const int64_t i = first + j;
-    int64_t q = i;
-    const int ipy = (int)(q % c.npy);
-    q /= c.npy;
-    const int ipx = (int)(q % c.npx);
-    q /= c.npx;
-    const int ify = (int)(q % c.nfy);
-    q /= c.nfy;
-    const int ifx = (int)(q % c.nfx);
-    const int iw = (int)(q / c.nfx);
+    IDX q = (IDX)i;
+    const int ipy = (int)(q % (IDX)c.npy);
+    q /= (IDX)c.npy;
+    const int ipx = (int)(q % (IDX)c.npx);
+    q /= (IDX)c.npx;
+    const int ify = (int)(q % (IDX)c.nfy);
+    q /= (IDX)c.nfy;
+    const int ifx = (int)(q % (IDX)c.nfx);
+    const int iw = (int)(q / (IDX)c.nfx);
     float uw = 0.5f, ufx = 0.5f, ufy = 0.5f, upx = 0.5f, upy = 0.5f;
     if (c.random) {
-      // counter (ray index, stream 0x1ce115, draw); key = seed
+      // one Philox call, counter (ray index, stream 0x1ce115, 0), key =
+      // seed: four uniforms from the top 24 bits of its words and a fifth
+      // from the low bytes of the first three
       const u32x4 a = philox4x32_10(
           u32x4{(uint32_t)i, (uint32_t)((uint64_t)i >> 32), 0x1ce115u, 0u}, k0, k1);
-      const u32x4 b = philox4x32_10(
-          u32x4{(uint32_t)i, (uint32_t)((uint64_t)i >> 32), 0x1ce115u, 1u}, k0, k1);
       uw = u01(a.x);
       ufx = u01(a.y);
       ufy = u01(a.z);
       upx = u01(a.w);
-      upy = u01(b.x);
+      upy = u01(((a.x & 0xffu) << 24) | ((a.y & 0xffu) << 16) | ((a.z & 0xffu) << 8));
     }
     const float* wv = reinterpret_cast<const float*>(c.wavelength);
     const float wl = fmaf(wv[iw + 1] - wv[iw], uw, wv[iw]);
@@ -169,8 +172,11 @@ extern "C" otx_status otx_cell_rays(const otx_cells* cells, int64_t first, int64
   if (!out->wavelength || !out->field_x || !out->field_y || !out->pupil_x || !out->pupil_y ||
       !out->intensity)
     return OTX_ERR_INVALID;
-  k_cell_rays<<<grid_for(count), 256, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
-      c, first, count, *out);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  if (total <= (int64_t)UINT32_MAX)
+    k_cell_rays<uint32_t><<<grid_for(count), 256, 0, st>>>(c, first, count, *out);
+  else
+    k_cell_rays<uint64_t><<<grid_for(count), 256, 0, st>>>(c, first, count, *out);
   return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
 }
 

@@ -34,7 +34,7 @@ import torch
 from . import _lib as L
 from .vectors import (Cartesian2dVectorArray, FunctionArray, SpectralPositionalVectorArray)
 
-__all__ = ["CellTables", "cell_tables", "image", "solid_angle_cells"]
+__all__ = ["CellTables", "ImagePlan", "cell_tables", "image", "solid_angle_cells"]
 
 
 def _direction(ax, ay):
@@ -145,6 +145,90 @@ def cell_tables(system, scene: FunctionArray, pupil=None, normalized_field: bool
     return CellTables(w, fx, fy, px, py, weight, area_p)
 
 
+class ImagePlan:
+    """An image simulation with its tables and device buffers made once:
+    :meth:`run` enqueues the chunks (cell rays, fused trace with binning)
+    and the exposure on the current stream and returns the electrons."""
+
+    def __init__(self, system, scene: FunctionArray, pupil=None, normalized_field: bool = True,
+                 normalized_pupil: bool = True, integrate: bool = True, random: bool = True,
+                 seed: int = 0, chunk: int = 1 << 24):
+        from . import _api
+
+        sensor = system.sensor
+        if sensor is None:
+            raise ValueError("image needs a sensor")
+        self.system = system
+        self.sensor = sensor
+        t = cell_tables(system, scene, pupil, normalized_field, normalized_pupil)
+        self.tables = t
+        nw, nfx, nfy, npx, npy = t.shape
+        w = t.wavelength
+        if integrate:
+            self.edges = np.array([w.min(), w.max()])
+            bins = (float(self.edges[0]), float(self.edges[1]), 1)
+        else:
+            if not np.allclose(np.diff(w), (w[-1] - w[0]) / nw, rtol=1e-6, atol=0):
+                raise ValueError("integrate=False needs uniformly spaced wavelength vertices")
+            self.edges = w
+            bins = (float(w[0]), float(w[-1]), nw)
+        dev = _api.device()
+
+        def dev_table(a: np.ndarray) -> torch.Tensor:
+            return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float32), device=dev)
+
+        self._tabs = [dev_table(a) for a in (t.wavelength, t.field_x, t.field_y, t.pupil_x,
+                                             t.pupil_y, t.weight, t.weight_pupil)]
+        cells = L.Cells()
+        (cells.wavelength, cells.field_x, cells.field_y, cells.pupil_x, cells.pupil_y,
+         cells.weight, cells.weight_pupil) = (_api.ptr(x) for x in self._tabs)
+        cells.nw, cells.nfx, cells.nfy, cells.npx, cells.npy = nw, nfx, nfy, npx, npy
+        cells.random = 1 if random else 0
+        cells.seed = int(seed) & (2**64 - 1)
+        self.cells = cells
+        self.seed = int(seed)
+        self.count = t.count
+        self.chunk = max(1, min(int(chunk), self.count))
+        self._buf = [torch.empty(self.chunk, dtype=torch.float32, device=dev) for _ in range(6)]
+        b = self._buf
+        self.trace = _api.PreparedTrace(
+            system, wavelength=b[0], field=Cartesian2dVectorArray(b[1], b[2]),
+            pupil=Cartesian2dVectorArray(b[3], b[4]), intensity=b[5], final_local=True,
+            image=True, wavelength_bins=bins, outputs=(), cos_moment=True)
+
+    @property
+    def launches(self) -> int:
+        """Kernels per :meth:`run`: per chunk the cell rays and the trace,
+        then the exposure."""
+        return 2 * ((self.count + self.chunk - 1) // self.chunk) + 1
+
+    def photons(self) -> tuple[torch.Tensor, torch.Tensor]:
+        """Photon image and flux-weighted cosine moment of the cells."""
+        from . import _api
+
+        for first in range(0, self.count, self.chunk):
+            n = min(self.chunk, self.count - first)
+            self.trace.grid.count = n
+            _api.cell_rays(self.cells, first, n, self.trace.grid)
+            self.trace.run(clear=first == 0)
+        return self.trace.flux, self.trace.moment
+
+    def run(self, noise: bool = True, timedelta=None, photons: bool = True) -> torch.Tensor:
+        flux, mom = self.photons()
+        direction = torch.where(flux > 0, mom / torch.where(flux > 0, flux, 1), 1)
+        return self.sensor.expose(flux, direction=direction, timedelta=timedelta, noise=noise,
+                                  seed=self.seed + 1, photons=photons, wavelength=self.edges)
+
+    def result(self, electrons: torch.Tensor) -> FunctionArray:
+        wx, wy = self.sensor.width_pixel_xy
+        nx, ny = self.sensor.num_pixel
+        pix = Cartesian2dVectorArray(np.linspace(-wx * nx / 2, wx * nx / 2, nx + 1),
+                                     np.linspace(-wy * ny / 2, wy * ny / 2, ny + 1))
+        return FunctionArray(
+            inputs=SpectralPositionalVectorArray(wavelength=self.edges, position=pix),
+            outputs=electrons)
+
+
 def image(system, scene: FunctionArray, pupil=None, normalized_field: bool = True,
           normalized_pupil: bool = True, integrate: bool = True, noise: bool = True,
           random: bool = True, seed: int = 0, timedelta=None, chunk: int = 1 << 24,
@@ -155,55 +239,6 @@ def image(system, scene: FunctionArray, pupil=None, normalized_field: bool = Tru
     ``[num_wavelength, num_pixel_x, num_pixel_y]``.  See the module
     docstring; ``random=False`` traces the cell centres (deterministic),
     ``seed`` keys the cell draws and the noise."""
-    from . import _api
-
-    sensor = system.sensor
-    if sensor is None:
-        raise ValueError("image needs a sensor")
-    t = cell_tables(system, scene, pupil, normalized_field, normalized_pupil)
-    nw, nfx, nfy, npx, npy = t.shape
-    w = t.wavelength
-    if integrate:
-        edges = np.array([w.min(), w.max()])
-        bins = (float(edges[0]), float(edges[1]), 1)
-    else:
-        if not np.allclose(np.diff(w), (w[-1] - w[0]) / nw, rtol=1e-6, atol=0):
-            raise ValueError("integrate=False needs uniformly spaced wavelength vertices")
-        edges = w
-        bins = (float(w[0]), float(w[-1]), nw)
-    dev = _api.device()
-
-    def dev_table(a: np.ndarray) -> torch.Tensor:
-        return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float32), device=dev)
-
-    tabs = [dev_table(a) for a in (t.wavelength, t.field_x, t.field_y, t.pupil_x, t.pupil_y,
-                                   t.weight, t.weight_pupil)]
-    cells = L.Cells()
-    (cells.wavelength, cells.field_x, cells.field_y, cells.pupil_x, cells.pupil_y, cells.weight,
-     cells.weight_pupil) = (_api.ptr(x) for x in tabs)
-    cells.nw, cells.nfx, cells.nfy, cells.npx, cells.npy = nw, nfx, nfy, npx, npy
-    cells.random = 1 if random else 0
-    cells.seed = int(seed) & (2**64 - 1)
-    total = t.count
-    n = max(1, min(int(chunk), total))
-    buf = [torch.empty(n, dtype=torch.float32, device=dev) for _ in range(6)]
-    field = Cartesian2dVectorArray(buf[1], buf[2])
-    pup = Cartesian2dVectorArray(buf[3], buf[4])
-    p = _api.PreparedTrace(system, wavelength=buf[0], field=field, pupil=pup, intensity=buf[5],
-                           final_local=True, image=True, wavelength_bins=bins, outputs=(),
-                           cos_moment=True)
-    for first in range(0, total, n):
-        count = min(n, total - first)
-        p.grid.count = count
-        _api.cell_rays(cells, first, count, p.grid)
-        p.run(clear=first == 0)
-    flux, mom = p.flux, p.moment
-    direction = torch.where(flux > 0, mom / torch.where(flux > 0, flux, 1), 1)
-    electrons = sensor.expose(flux, direction=direction, timedelta=timedelta, noise=noise,
-                              seed=seed + 1, photons=photons, wavelength=edges)
-    wx, wy = sensor.width_pixel_xy
-    nx, ny = sensor.num_pixel
-    pix = Cartesian2dVectorArray(np.linspace(-wx * nx / 2, wx * nx / 2, nx + 1),
-                                 np.linspace(-wy * ny / 2, wy * ny / 2, ny + 1))
-    return FunctionArray(inputs=SpectralPositionalVectorArray(wavelength=edges, position=pix),
-                         outputs=electrons)
+    plan = ImagePlan(system, scene, pupil, normalized_field, normalized_pupil, integrate,
+                     random, seed, chunk)
+    return plan.result(plan.run(noise=noise, timedelta=timedelta, photons=photons))

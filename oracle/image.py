@@ -16,8 +16,10 @@ the rays traced by this package's float64 oracle (oracle/trace.py).
   form of the triangle's solid angle);
 * ``cell_centers(axis)``: the mean of the two vertices along each axis;
   with ``random=True`` a uniformly drawn point of the cell, the draws here
-  being the same Philox4x32-10 uniforms the device uses (oracle/batch.py),
-  one draw per axis shared by every coordinate of the ray.
+  being the same Philox4x32-10 uniforms the device uses (oracle/batch.py:
+  one generator call per ray, four uniforms from the top 24 bits of its
+  words, the fifth from the low bytes of the first three), one draw per
+  axis shared by every coordinate of the ray.
 """
 
 from __future__ import annotations
@@ -93,14 +95,15 @@ def cell_tables(system, wavelength, field_x, field_y, radiance, pupil_x=(-1.0, 1
     return w, fx, fy, px, py, rad * np.diff(w)[:, None, None] * af, ap
 
 
-def cell_inputs(tables, random=True, seed=0):
-    """Input grid of every cell (ray order wavelength, field x, field y,
-    pupil x, pupil y, the last fastest)."""
+def cell_inputs(tables, random=True, seed=0, first=0, count=None):
+    """Input grid of cells [first, first + count) (all by default; ray order
+    wavelength, field x, field y, pupil x, pupil y, the last fastest)."""
     w, fx, fy, px, py, weight, wp = tables
     nw, nfx, nfy = weight.shape
     npx, npy = wp.shape[1:]
-    n = nw * nfx * nfy * npx * npy
-    i = np.arange(n, dtype=np.uint64)
+    total = nw * nfx * nfy * npx * npy
+    n = total - first if count is None else count
+    i = np.arange(first, first + n, dtype=np.uint64)
     q = i.astype(np.int64)
     ipy = q % npy
     q //= npy
@@ -113,9 +116,11 @@ def cell_inputs(tables, random=True, seed=0):
     if random:
         k0, k1 = seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF
         a = philox4x32_10(i & MASK, i >> np.uint64(32), 0x1CE115, 0, k0, k1)
-        b = philox4x32_10(i & MASK, i >> np.uint64(32), 0x1CE115, 1, k0, k1)
         uw, ufx, ufy, upx = (u01(v).astype(np.float64) for v in a)
-        upy = u01(b[0]).astype(np.float64)
+        ff = np.uint64(0xFF)
+        low = ((a[0] & ff) << np.uint64(24)) | ((a[1] & ff) << np.uint64(16)) | (
+            (a[2] & ff) << np.uint64(8))
+        upy = u01(low).astype(np.float64)
     else:
         uw = ufx = ufy = upx = upy = np.full(n, 0.5)
 
