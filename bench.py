@@ -625,6 +625,88 @@ def run_image(args, rank: int, world: int) -> None:
         }), flush=True)
 
 
+def _cpu_stops_worker(args):
+    wavelength, = args
+    from optika_gb300 import configs
+    from oracle import stops as OS
+
+    OS.extents(configs.stop_grazing(), wavelength)
+    return (1,)
+
+
+def run_stops(args, rank: int, world: int) -> None:
+    """The stop solver: field and pupil extents of the grazing-incidence
+    spectrograph at 16 wavelengths (21 x 21 boundary ray pairs each, Newton
+    to convergence, the backward trace), all wavelengths in one batched
+    solve.  Host-driven and latency-bound: a step is the public call
+    ``extents_many`` with the cache cleared; replicas under torchrun."""
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from optika_gb300 import configs
+    from optika_gb300.stops import extents_many
+
+    from optika_gb300 import stops as stops_mod
+
+    system = configs.stop_grazing()
+    wls = np.linspace(500.0, 600.0, 16)
+    launches = [0]
+    trace = stops_mod._trace
+
+    def counted(*a, **k):  # each call is one otx_trace_rays launch
+        launches[0] += 1
+        return trace(*a, **k)
+
+    stops_mod._trace = counted
+
+    def step():
+        system.__dict__.pop("_stop_extents", None)
+        return extents_many(system, wls)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    launches[0] = 0
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    value = world * len(wls) / (ms * 1e-3)
+    traces = launches[0]
+    pk, pk_kind = peaks()
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cores = len(os.sched_getaffinity(0))
+        jobs = [(float(w),) for w in np.linspace(500.0, 600.0, cores)]
+        solves, wall = _cpu_pool(_cpu_stops_worker, jobs, cores)
+        cpu = {"value": solves / wall, "unit": "solves/s", "cores": cores, "kind": "port",
+               "sample": f"{len(jobs)} wavelengths, one float64 solve per process "
+                         f"({wall:.1f} s)"}
+    if rank == 0:
+        print(json.dumps({
+            "metric": "stop solves/s (field and pupil extents per wavelength)",
+            "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 trace, f64 Newton updates",
+            "data": "synthetic (the grazing spectrograph test system)",
+            "config": {"workload": "stop-solver", "wavelengths": len(wls),
+                       "boundary_pairs": 441, "system": "grazing spectrograph"},
+            "roofline": {"bound": "hbm", "achieved": None, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                         "frac": None, "traffic": None, "peak_kind": pk_kind,
+                         "note": "latency-bound: a few thousand rays per launch, one host "
+                                 "convergence check per Newton iteration"},
+            "e2e": {"value": value, "unit": "solves/s", "ms_per_step": ms,
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 16 * len(wls) * 8},
+            "cpu_baseline": cpu, "gpu_launches": traces, "clocks": clk,
+        }), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -638,7 +720,8 @@ def main() -> None:
                     help="rays per step of the reference (CPU) arm")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="precision",
-                    choices=["precision", "surrogate", "batched", "multilayer", "image"])
+                    choices=["precision", "surrogate", "batched", "multilayer", "image",
+                             "stops"])
     ap.add_argument("--configs", type=int, default=4096, help="batched workload configurations")
     ap.add_argument("--samples", type=int, default=10_000_000,
                     help="multilayer workload samples per step")
@@ -669,6 +752,9 @@ def main() -> None:
         return
     if args.workload == "image":
         run_image(args, rank, world)
+        return
+    if args.workload == "stops":
+        run_stops(args, rank, world)
         return
 
     import torch

@@ -147,7 +147,7 @@ def area_effective(system, wavelength=None, field=None, pupil=None, normalized_f
     pupil cell at a uniformly drawn point of the cell (its centre when not
     ``random``), weighted by the cell's area; the intensity of the
     unvignetted rays summed over the pupil and averaged over the field."""
-    from .stops import extents
+    from .stops import extents, extents_many
 
     g = system.grid_input
     if wavelength is None:
@@ -161,6 +161,8 @@ def area_effective(system, wavelength=None, field=None, pupil=None, normalized_f
     vx, vy = _axis(pupil.x, "pupil x"), _axis(pupil.y, "pupil y")
     nw, npx, npy = len(w), len(vx) - 1, len(vy) - 1
     # pupil vertices at each wavelength (denormalised by the stop solver)
+    if normalized_pupil:
+        extents_many(system, w)  # all wavelengths in one batched solve
     PX = np.empty((nw, npx + 1))
     PY = np.empty((nw, npy + 1))
     for k in range(nw):

@@ -104,7 +104,7 @@ def _vertices(v, name: str) -> np.ndarray:
 def cell_tables(system, scene: FunctionArray, pupil=None, normalized_field: bool = True,
                 normalized_pupil: bool = True) -> CellTables:
     """Tables of the scene's cells (host, float64)."""
-    from .stops import extents
+    from .stops import extents, extents_many
 
     w = _vertices(scene.inputs.wavelength, "wavelength")
     fxn = _vertices(scene.inputs.position.x, "field x")
@@ -119,6 +119,9 @@ def cell_tables(system, scene: FunctionArray, pupil=None, normalized_field: bool
     if isinstance(rad, torch.Tensor):
         rad = rad.detach().double().cpu().numpy()
     rad = np.broadcast_to(np.asarray(rad, dtype=np.float64), (nw, nfx, nfy))
+
+    if normalized_field or normalized_pupil:
+        extents_many(system, w)  # every wavelength vertex in one batched solve
 
     def per_wavelength(v: np.ndarray, which: int, comp: int, normalized: bool) -> np.ndarray:
         out = np.empty((nw + 1, len(v)))

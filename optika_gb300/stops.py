@@ -31,9 +31,7 @@ import numpy as np
 import torch
 
 from . import transforms
-from ._api import device, propagate_rays
-from .rays import RayVectorArray
-from .vectors import Cartesian3dVectorArray
+from ._api import device
 
 SAMPLES_STOP = 21
 MAX_ITER = 60
@@ -80,32 +78,59 @@ def _sag(sag, x: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
     return sag(Cartesian2dVectorArray(x.float(), y.float())).to(torch.float64)
 
 
-def _trace(surfaces: Sequence, p: torch.Tensor, d: torch.Tensor, wavelength: float):
+def _lower(surfaces: Sequence):
+    """The descriptor of ``surfaces`` for repeated traces within one solve."""
+    from . import _lib as L
+    from ._lower import lower_surfaces
+
+    return lower_surfaces(list(surfaces), pre=np.eye(4), final=None, input_mode=L.INPUT_RAYS,
+                          device=device())
+
+
+def _trace(surfaces: Sequence, p: torch.Tensor, d: torch.Tensor, wavelength, lowering=None):
     """Rays [3, N] (system frame, float64 on the host side of the kernel
-    call) through ``surfaces``: one launch of the trace kernel."""
+    call) through ``surfaces``: one launch of the trace kernel
+    (otx_trace_rays) with only the position, direction and wavelength given
+    (the other ray fields take their defaults) and only position and
+    direction written.  ``wavelength`` is one value or a tensor [N];
+    ``lowering`` is the descriptor from :func:`_lower`, made once per
+    solve."""
+    import ctypes
+
+    from . import _api
+    from . import _lib as L
+
     n = p.shape[1]
     dev = p.device
-    rays = RayVectorArray(
-        wavelength=torch.full((n,), float(wavelength), device=dev),
-        position=Cartesian3dVectorArray(*(p[i].float() for i in range(3))),
-        direction=Cartesian3dVectorArray(*(d[i].float() for i in range(3))),
-        intensity=torch.ones(n, device=dev),
-        attenuation=torch.zeros(n, device=dev),
-        index_refraction=torch.ones(n, device=dev),
-        unvignetted=torch.ones(n, dtype=torch.bool, device=dev),
-        opl=torch.zeros(n, dtype=torch.float64, device=dev),
-    )
-    out = propagate_rays(list(surfaces), rays)
-    po = torch.stack([out.position.x, out.position.y, out.position.z]).to(torch.float64)
-    do = torch.stack([out.direction.x, out.direction.y, out.direction.z]).to(torch.float64)
-    return po, do
+    lw = lowering if lowering is not None else _lower(surfaces)
+    wl = (wavelength.to(device=dev, dtype=torch.float32).contiguous()
+          if isinstance(wavelength, torch.Tensor)
+          else torch.full((n,), float(wavelength), device=dev))
+    pf = p.to(torch.float32).contiguous()
+    df = d.to(torch.float32).contiguous()
+    inp = dict(px=pf[0], py=pf[1], pz=pf[2], dx=df[0], dy=df[1], dz=df[2], wavelength=wl)
+    out = torch.empty((6, n), dtype=torch.float32, device=dev)
+    outs = dict(px=out[0], py=out[1], pz=out[2], dx=out[3], dy=out[4], dz=out[5])
+    L.check(L.load().otx_trace_rays(
+        ctypes.byref(lw.sys), ctypes.byref(_api._rays_struct(inp, n)),
+        ctypes.byref(_api._rays_struct(outs, n)), None, ctypes.byref(L.Launch()),
+        _api.stream_handle()), "otx_trace_rays")
+    o = out.to(torch.float64)
+    return o[:3], o[3:]
 
 
-def stops_only(system, wavelength: float, samples_pupil: int = SAMPLES_STOP,
+def stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
                samples_field: int = SAMPLES_STOP) -> dict:
     """Rays (system frame, [3, first wire, last wire]) from the first stop
     that strike every point of the last stop's boundary
-    (optika/systems/_sequential.py:396-693)."""
+    (optika/systems/_sequential.py:396-693).  ``wavelength`` may be a 1-D
+    array: every wavelength is solved in the same Newton iterations (one
+    trace launch per iteration for all of them) and the arrays gain a
+    wavelength axis after the first, [3, wavelength, first wire, last
+    wire]."""
+    scalar = np.ndim(wavelength) == 0
+    wls = np.atleast_1d(np.asarray(wavelength, dtype=np.float64))
+    nw = len(wls)
     surfaces = system.surfaces_all
     ip = [i for i, s in enumerate(surfaces) if s.is_pupil_stop]
     jf = [i for i, s in enumerate(surfaces) if s.is_field_stop]
@@ -179,9 +204,15 @@ def stops_only(system, wavelength: float, samples_pupil: int = SAMPLES_STOP,
         tol = max(1e-9 * unit, 4e-7 * unit)
         dx = 1e-4 if variable == "direction" else 1e-4 * unit
         Tl = _inverse(_matrix(s_last.transformation))
-        n = shape[0] * shape[1]
-        pos_f = pos.reshape(3, n)
-        dir_f = dirn.reshape(3, n)
+        # every wavelength repeats the grid (wavelength-major)
+        n = nw * shape[0] * shape[1]
+        pos_f = pos.reshape(3, -1).repeat(1, nw)
+        dir_f = dirn.reshape(3, -1).repeat(1, nw)
+        tx = tx.repeat(nw)
+        ty = ty.repeat(nw)
+        wl_f = torch.as_tensor(wls, dtype=f64, device=dev).repeat_interleave(shape[0] * shape[1])
+
+        lw_sub = _lower(sub[1:])
 
         def residuals(xs, ys):
             """Residuals of len(xs) / n stacked evaluations in one launch."""
@@ -190,7 +221,7 @@ def stops_only(system, wavelength: float, samples_pupil: int = SAMPLES_STOP,
             d = dir_f.repeat(1, k)
             v = d if variable == "direction" else p
             v[0], v[1], v[2] = xs, ys, zf(xs, ys)
-            po, do = _trace(sub[1:], p, d, wavelength)
+            po, do = _trace(sub[1:], p, d, wl_f.repeat(k), lw_sub)
             if target == "direction":
                 c = _apply(Tl, do, point=False)
             else:
@@ -225,16 +256,19 @@ def stops_only(system, wavelength: float, samples_pupil: int = SAMPLES_STOP,
                 f"{s_first.name!r} and {s_last.name!r}")
         v = dir_f if variable == "direction" else pos_f
         v[0], v[1], v[2] = x, y, zf(x, y)
-        out = dict(position=pos_f.reshape((3,) + shape), direction=dir_f.reshape((3,) + shape))
+        full = (3,) + ((nw,) if not scalar else ()) + shape
+        out = dict(position=pos_f.reshape(full), direction=dir_f.reshape(full),
+                   wavelength=wl_f.reshape(full[1:]))
     return out
 
 
-def rayfunction_stops(system, wavelength: float, samples_pupil: int = SAMPLES_STOP,
+def rayfunction_stops(system, wavelength, samples_pupil: int = SAMPLES_STOP,
                       samples_field: int = SAMPLES_STOP) -> dict:
     """The stop rays traced back to the object surface, directions pointing
     into the system, with the field and pupil grids they give: angles
     (rad) for the side at infinity, positions (mm) for the other
-    (optika/systems/_sequential.py:695-754)."""
+    (optika/systems/_sequential.py:695-754).  A 1-D ``wavelength`` adds a
+    leading wavelength axis to every grid."""
     st = stops_only(system, wavelength, samples_pupil, samples_field)
     surfaces = system.surfaces_all
     ip = max(i for i, s in enumerate(surfaces) if s.is_pupil_stop)
@@ -242,7 +276,7 @@ def rayfunction_stops(system, wavelength: float, samples_pupil: int = SAMPLES_ST
     sub = surfaces[min(ip, jf)::-1]
     p, d = st["position"], st["direction"]
     shape = p.shape[1:]
-    po, do = _trace(sub, p.reshape(3, -1), d.reshape(3, -1), wavelength)
+    po, do = _trace(sub, p.reshape(3, -1), d.reshape(3, -1), st["wavelength"].reshape(-1))
     obj = sub[-1]
     Mi = _inverse(_matrix(obj.transformation))
     pl = _apply(Mi, po)
@@ -270,16 +304,25 @@ def extents(system, wavelength: float) -> tuple:
     """(field_min, field_max, pupil_min, pupil_max), each an (x, y) pair of
     floats, cached on the system per wavelength
     (optika/systems/_sequential.py:755-799)."""
+    return extents_many(system, [wavelength])[0]
+
+
+def extents_many(system, wavelengths) -> list[tuple]:
+    """:func:`extents` of several wavelengths; the ones not yet cached are
+    solved together (one batched Newton solve, see :func:`stops_only`)."""
     cache = system.__dict__.setdefault("_stop_extents", {})
-    key = float(wavelength)
-    if key not in cache:
-        st = rayfunction_stops(system, key)
+    keys = [float(w) for w in np.atleast_1d(np.asarray(wavelengths, dtype=np.float64))]
+    todo = sorted({k for k in keys if k not in cache})
+    if todo:
+        st = rayfunction_stops(system, np.array(todo))
         f, q = st["field"], st["pupil"]
-        cache[key] = ((float(f[0].min()), float(f[1].min())),
-                      (float(f[0].max()), float(f[1].max())),
-                      (float(q[0].min()), float(q[1].min())),
-                      (float(q[0].max()), float(q[1].max())))
-    return cache[key]
+        red = [(a.reshape(len(todo), -1).amin(1).cpu().numpy(),
+                a.reshape(len(todo), -1).amax(1).cpu().numpy()) for a in (*f, *q)]
+        for j, k in enumerate(todo):
+            (fx0, fx1), (fy0, fy1), (qx0, qx1), (qy0, qy1) = red
+            cache[k] = ((float(fx0[j]), float(fy0[j])), (float(fx1[j]), float(fy1[j])),
+                        (float(qx0[j]), float(qy0[j])), (float(qx1[j]), float(qy1[j])))
+    return [cache[k] for k in keys]
 
 
 def _values(x):
@@ -298,7 +341,7 @@ def denormalize(system, wavelength, field, pupil, normalized_field: bool,
     ws = np.unique(_values(wavelength))
     if len(ws) > 64:
         raise ValueError("normalised coordinates support at most 64 distinct wavelengths")
-    ext = [extents(system, w) for w in ws]
+    ext = extents_many(system, ws)
 
     def table(which: int, comp: int):
         lo = np.array([e[which][comp] for e in ext])
@@ -334,4 +377,5 @@ def denormalize(system, wavelength, field, pupil, normalized_field: bool,
     return (fx, fy), (qx, qy)
 
 
-__all__ = ["anchor_surface", "stops_only", "rayfunction_stops", "extents", "denormalize"]
+__all__ = ["anchor_surface", "stops_only", "rayfunction_stops", "extents", "extents_many",
+           "denormalize"]
