@@ -180,7 +180,7 @@ def run_reference(args, rank: int, world: int) -> None:
 def run_surrogate(args, rank: int, world: int) -> None:
     """The learned form: a 9-256x4-3 BF16 MLP surrogate of the batched
     spectrograph's ray map over 64 configurations, trained on 5e7 rays the
-    plain batched kernel traces, judged on 1e6 held-out rays, then used to
+    plain batched kernel traces, evaluated on 1e6 held-out rays, then used to
     simulate the sensor images of 1e9 rays with plain-trace fallback.  The
     same 1e9 rays through the plain batched kernel give the comparison.
     Single GPU (replicas under torchrun)."""

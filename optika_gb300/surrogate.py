@@ -1,5 +1,5 @@
 """Learned surrogate of a batched trace's ray map, trained and run on the
-tensor cores, with the plain trace as fallback and judge.
+tensor cores, with the plain trace as its fallback and its accuracy reference.
 
 The reference has no counterpart: this is the learned part built on top of
 the batched spectrograph trace (``optika_gb300.batch``).  For every ray of a
