@@ -79,6 +79,18 @@ def _call_rays(lib, sys_, count=0):
         (lambda s: (setattr(s.surfaces[0], "rule_type", L.RULE_POLY1D),
                     setattr(s.surfaces[0], "rule_num_terms", 9)), L.ERR_SIZE),
         (lambda s: setattr(s.layers[0], "table", 3), L.ERR_INVALID),
+        (lambda s: setattr(s.surfaces[0], "sag_type", L.SAG_CYLINDER + 1), L.ERR_UNSUPPORTED),
+        (lambda s: setattr(s.surfaces[0], "mat_type", L.MAT_MEASURED_MIRROR + 1),
+         L.ERR_UNSUPPORTED),
+        (lambda s: (setattr(s.surfaces[0], "mat_type", L.MAT_MEASURED_MIRROR),
+                    setattr(s.surfaces[0], "mat_table", 16)), L.ERR_INVALID),
+        (lambda s: (setattr(s.surfaces[0], "mat_type", L.MAT_MEASURED_MIRROR),
+                    setattr(s.surfaces[0], "mat_table", 0)), L.ERR_INVALID),  # empty table
+        (lambda s: (setattr(s.surfaces[0], "rule_type", L.RULE_CONSTANT),
+                    setattr(s.surfaces[0], "rule_eff_type", 7)), L.ERR_UNSUPPORTED),
+        (lambda s: (setattr(s.surfaces[0], "rule_type", L.RULE_CONSTANT),
+                    setattr(s.surfaces[0], "rule_eff_type", L.RULE_EFF_MEASURED),
+                    setattr(s.surfaces[0], "rule_table", -1)), L.ERR_INVALID),
         (lambda s: (setattr(s.stacks[0], "pre_count", 5),
                     setattr(s.stacks[0], "pre_begin", L.MAX_LAYERS - 2)), L.ERR_INVALID),
     ],
@@ -214,3 +226,41 @@ def test_fused_surrogate_validation(built_library):
     assert call(net_=net2) == L.ERR_INVALID
     s2 = _system(4)
     assert call(sys_=s2) == L.ERR_UNSUPPORTED  # outputs must be in the sensor frame
+
+
+def test_rulings_cells_expose_reduce_validation(built_library):
+    """The entry points added for the rulings, the forward model and the
+    calibration fits reject bad arguments on the host."""
+    lib = built_library
+    s = _system()
+    r = L.Rays()
+    # rulings: no rulings on the surface, bad mode
+    assert lib.otx_rulings_eval(ctypes.byref(s), 0, ctypes.byref(r), ctypes.byref(r), None,
+                                None, None) == L.ERR_INVALID
+    s.surfaces[0].rule_type = L.RULE_CONSTANT
+    assert lib.otx_rulings_eval(ctypes.byref(s), 2, ctypes.byref(r), ctypes.byref(r), None,
+                                None, None) == L.ERR_INVALID
+    assert lib.otx_rulings_eval(ctypes.byref(s), 0, ctypes.byref(r), ctypes.byref(r), None,
+                                None, None) == L.OK  # empty input, no launch
+    r.count = 4
+    assert lib.otx_rulings_eval(ctypes.byref(s), 0, ctypes.byref(r), ctypes.byref(r), None,
+                                None, None) == L.ERR_INVALID  # missing pointers
+    # cells: bad dimensions, range past the end, missing tables
+    c = L.Cells()
+    g = L.Grid()
+    assert lib.otx_cell_rays(ctypes.byref(c), 0, 1, ctypes.byref(g), None) == L.ERR_INVALID
+    c.nw = c.nfx = c.nfy = c.npx = c.npy = 2
+    assert lib.otx_cell_rays(ctypes.byref(c), 30, 3, ctypes.byref(g), None) == L.ERR_SIZE
+    assert lib.otx_cell_rays(ctypes.byref(c), 0, 0, ctypes.byref(g), None) == L.OK
+    assert lib.otx_cell_rays(ctypes.byref(c), 0, 8, ctypes.byref(g), None) == L.ERR_INVALID
+    assert lib.otx_cell_rays(ctypes.byref(c), -1, 8, ctypes.byref(g), None) == L.ERR_INVALID
+    # exposure
+    assert lib.otx_expose(None, None, -1, 1.0, 0.0, 1, 0, None) == L.ERR_INVALID
+    assert lib.otx_expose(None, None, 0, 1.0, 0.0, 1, 0, None) == L.OK
+    assert lib.otx_expose(None, None, 5, 1.0, 0.0, 1, 0, None) == L.ERR_INVALID
+    # pupil reduction: count must be groups x per_group, pointers present
+    rr = L.Rays()
+    rr.count = 10
+    assert lib.otx_pupil_reduce(ctypes.byref(rr), 2, 5, None, None) == L.ERR_INVALID
+    assert lib.otx_pupil_reduce(ctypes.byref(rr), 0, 5, None, None) == L.OK
+    assert lib.otx_pupil_reduce(ctypes.byref(rr), 2, 0, None, None) == L.ERR_INVALID
