@@ -87,6 +87,22 @@ def test_effective_area_interpolation():
     assert np.allclose(m(np.array([5.0, 15.0, 25.0, 35.0])), [1.0, 2.0, 2.5, 2.0])
 
 
+def test_oracle_distortion_has_the_paraboloid_plate_scale():
+    """The Newtonian's paraboloid (R = -800 mm) has a focal length of 400 mm:
+    the mean sensor position of a field point moves 400 mm per radian of
+    field angle (to 1 %: the pupil-averaged coma shifts the centroid), odd
+    in the angle."""
+    s = configs.newtonian()
+    f = np.linspace(-0.1, 0.1, 5) * DEG
+    p = np.linspace(-40.0, 40.0, 9)
+    o = OF.distortion(s, np.array([550.0]), f, f, p, p)
+    mx, my = o["sensor"]
+    for line in (mx[0, :, 2], my[0, 2, :]):
+        slope = np.polyfit(f, line, 1)[0]
+        assert abs(abs(slope) / 400.0 - 1) < 0.01
+        assert np.allclose(line, -line[::-1], atol=1e-9)
+
+
 # ---------------------------------------------------------------- GPU
 
 

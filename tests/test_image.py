@@ -52,6 +52,40 @@ def test_solid_angles_agree_and_reach_the_coordinate_limit():
     assert abs(imaging.solid_angle_cells(ax, ay)[0, 0] / exact - 1) < 1e-5
 
 
+def test_solid_angle_total_converges_to_the_coordinate_integral():
+    """The cells of the square field [-a, a]^2 of field angles cover
+    int cos(ay) dax day = 4 a sin(a); the great-circle cells converge to it
+    quadratically."""
+    a = 5 * DEG
+    exact = 4 * a * math.sin(a)
+    errs = [abs(imaging.solid_angle_cells(np.linspace(-a, a, n + 1),
+                                          np.linspace(-a, a, n + 1)).sum() / exact - 1)
+            for n in (16, 64)]
+    assert errs[1] < 1e-6 and errs[0] / errs[1] > 12
+
+
+def test_image_flux_is_radiance_times_etendue():
+    """Every ray of a system without apertures reaches the sensor: the photon
+    image holds radiance x wavelength width x field solid angle x pupil
+    area, in the oracle's trace of the product's cell tables as in the
+    tables themselves."""
+    sensor = ok.sensors.ImagingSensor(width_pixel=0.1, num_pixel=(512, 512),
+                                      transformation=ok.transforms.Translation(z=100.0))
+    s = ok.systems.SequentialSystem(surfaces=[], sensor=sensor)
+    a = 0.5 * DEG
+    w = np.linspace(500.0, 600.0, 3)
+    f = np.linspace(-a, a, 17)
+    v = np.linspace(-5.0, 5.0, 9)
+    scene = FunctionArray(inputs=SpectralPositionalVectorArray(wavelength=w, position=V2(f, f)),
+                          outputs=np.ones((2, 16, 16)))
+    t = imaging.cell_tables(s, scene, V2(v, v), False, False)
+    tab = OI.cell_tables(s, w, f, f, scene.outputs, v, v, False, False)
+    img, _ = OI.photon_image(s, OI.cell_inputs(tab, random=True, seed=3), (500.0, 600.0, 1))
+    expect = 100.0 * 4 * a * math.sin(a) * 10.0**2
+    assert abs(img.sum() / expect - 1) < 1e-6
+    assert abs(t.weight.sum() * t.weight_pupil[0].sum() / expect - 1) < 1e-6
+
+
 def test_cell_tables_match_the_oracle_in_physical_coordinates():
     s = configs.newtonian()
     rng = np.random.default_rng(3)
