@@ -139,8 +139,17 @@ def cell_tables(system, scene: FunctionArray, pupil=None, normalized_field: bool
     px = per_wavelength(pxn, 2, 0, normalized_pupil)
     py = per_wavelength(pyn, 2, 1, normalized_pupil)
     infinity = system.object_is_at_infinity
-    area_f = np.stack([_areas(fx[k], fy[k], angular=infinity) for k in range(nw + 1)])
-    area_p = np.stack([_areas(px[k], py[k], angular=not infinity) for k in range(nw + 1)])
+    memo: dict = {}
+
+    def areas(x: np.ndarray, y: np.ndarray, angular: bool) -> np.ndarray:
+        # physical grids repeat at every wavelength vertex: compute each once
+        key = (x.tobytes(), y.tobytes(), angular)
+        if key not in memo:
+            memo[key] = _areas(x, y, angular)
+        return memo[key]
+
+    area_f = np.stack([areas(fx[k], fy[k], infinity) for k in range(nw + 1)])
+    area_p = np.stack([areas(px[k], py[k], not infinity) for k in range(nw + 1)])
     # cell_centers along the wavelength axis: mean of the two vertices
     area_f = (area_f[:-1] + area_f[1:]) / 2
     area_p = (area_p[:-1] + area_p[1:]) / 2
