@@ -81,6 +81,16 @@ def test_simple_distortion_model_is_exactly_invertible():
     assert np.isclose(d.position.x[1] - m.distort(SP(550.0, V2(0.4, -0.2))).position.x, 5.0)
 
 
+def test_fits_need_grids():
+    s = configs.newtonian()
+    with pytest.raises(ValueError, match="grids"):
+        s.distortion()
+    with pytest.raises(ValueError, match="grids"):
+        s.vignetting(wavelength=np.array([550.0]))
+    with pytest.raises(ValueError, match="1-D"):
+        s.distortion(np.ones((2, 2)), V2(np.zeros(3), np.zeros(3)), V2(np.zeros(3), np.zeros(3)))
+
+
 def test_effective_area_interpolation():
     m = ok.radiometry.InterpolatedEffectiveAreaModel(np.array([10.0, 20.0, 30.0]),
                                                      np.array([1.0, 3.0, 2.0]))

@@ -120,6 +120,18 @@ def test_oracle_cell_samples_lie_in_their_cells():
     assert not np.allclose(r["field_x"], c["field_x"])
 
 
+def test_argument_checks_before_any_device_work():
+    s = configs.newtonian()
+    no_sensor = ok.systems.SequentialSystem(surfaces=s.surfaces, object=s.object)
+    with pytest.raises(ValueError, match="sensor"):
+        no_sensor.image(_scene(), pupil=_pupil(), normalized_field=False,
+                        normalized_pupil=False)
+    one = _scene()
+    one.inputs.wavelength = np.array([550.0])
+    with pytest.raises(ValueError, match="vertices"):
+        s.image(one, pupil=_pupil(), normalized_field=False, normalized_pupil=False)
+
+
 def test_integrate_false_needs_uniform_wavelengths():
     s = configs.newtonian()
     scene = _scene()
