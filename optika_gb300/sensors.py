@@ -122,6 +122,31 @@ class ImagingSensor(AbstractSurface):
         dt = self.timedelta_exposure if timedelta is None else timedelta
         return expose(img, float(dt), float(self.read_noise), noise, seed)
 
+    def photons_absorbed(self, image, direction=1, timedelta=None):
+        """The photon flux absorbed in each pixel from an electron image, the
+        deterministic inverse of :meth:`expose` (optika/sensors/_sensors.py:
+        254-315): the ideal material yields one electron per photon
+        (optika/sensors/materials/_materials.py:1627-1633), so this divides
+        by the exposure time.  Elementwise torch arithmetic on the image's
+        device."""
+        import torch
+
+        img = image if isinstance(image, torch.Tensor) else torch.as_tensor(
+            np.asarray(image, dtype=np.float32))
+        dt = self.timedelta_exposure if timedelta is None else timedelta
+        return img / dt
+
+    def uncertainty(self, image, direction=1):
+        """Standard deviation of the noise of an electron image
+        (optika/sensors/_sensors.py:317-372): the ideal material's shot
+        noise sqrt(electrons) (optika/sensors/materials/_materials.py:
+        1635-1644) and the read noise, added in quadrature."""
+        import torch
+
+        img = image if isinstance(image, torch.Tensor) else torch.as_tensor(
+            np.asarray(image, dtype=np.float32))
+        return torch.sqrt(img + float(self.read_noise) ** 2)
+
     def measure(self, rays, wavelength=None, where=True, timedelta=None, noise: bool = True,
                 seed: int = 0):
         """:meth:`collect` then :meth:`expose` (optika/sensors/_sensors.py:

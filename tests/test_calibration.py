@@ -113,6 +113,17 @@ def test_oracle_distortion_has_the_paraboloid_plate_scale():
         assert np.allclose(line, -line[::-1], atol=1e-9)
 
 
+def test_oracle_vignetting_has_unit_mean():
+    """optika/systems/_sequential_test.py:344-350: the relative illumination
+    averages to one over the field points with unvignetted rays."""
+    s = configs.newtonian()
+    f = np.linspace(-0.12, 0.12, 5) * DEG
+    p = np.linspace(-48.0, 48.0, 9)
+    v = OF.vignetting(s, np.array([450.0, 650.0]), f, f, p, p)
+    for k in range(2):
+        assert abs(v["illumination"][k][v["where"][k]].mean() - 1) < 1e-12
+
+
 # ---------------------------------------------------------------- GPU
 
 
@@ -163,6 +174,8 @@ def test_vignetting_matches_oracle(cuda):
     o = OF.vignetting(s, w, fx, fy, px, py)
     assert np.array_equal(m.where, o["where"])
     assert np.abs(m.illumination - o["illumination"]).max() < 2 / (17 * 17)
+    for k in range(len(w)):
+        assert abs(m.illumination[k][m.where[k]].mean() - 1) < 1e-12
     q = SP(np.array([550.0]), V2(np.array([0.03 * DEG]), np.array([-0.05 * DEG])))
     assert abs(m(q)[0] - o["fit"](q.wavelength, q.position.x, q.position.y)[0][0]) < 1e-2
 

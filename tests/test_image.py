@@ -132,6 +132,18 @@ def test_argument_checks_before_any_device_work():
         s.image(one, pupil=_pupil(), normalized_field=False, normalized_pupil=False)
 
 
+def test_photons_absorbed_and_uncertainty_of_the_ideal_sensor():
+    """optika/sensors/_sensors_test.py:96-134: photons_absorbed inverts
+    expose (one electron per photon, divided by the exposure time); the
+    uncertainty is sqrt(electrons + read_noise^2)."""
+    sensor = ok.sensors.ImagingSensor(width_pixel=0.01, num_pixel=(4, 4),
+                                      timedelta_exposure=2.0, read_noise=3.0)
+    e = torch.tensor([[0.0, 4.0], [16.0, 100.0]])
+    assert torch.equal(sensor.photons_absorbed(e), e / 2.0)
+    assert torch.equal(sensor.photons_absorbed(e, timedelta=4.0), e / 4.0)
+    assert torch.allclose(sensor.uncertainty(e), torch.sqrt(e + 9.0))
+
+
 def test_integrate_false_needs_uniform_wavelengths():
     s = configs.newtonian()
     scene = _scene()
@@ -239,6 +251,15 @@ def test_expose_read_noise_and_noiseless(cuda):
     assert abs(e.std().item() / 3.0 - 1) < 0.01
     img = torch.rand((1, 1000, 1000), device=cuda)
     assert torch.equal(sensor.expose(img, noise=False, timedelta=2.5), img * 2.5)
+
+
+@pytest.mark.gpu
+def test_photons_absorbed_inverts_expose(cuda):
+    sensor = ok.sensors.ImagingSensor(width_pixel=0.01, num_pixel=(64, 64),
+                                      timedelta_exposure=3.0)
+    img = torch.rand((1, 64, 64), device=cuda) * 100
+    back = sensor.photons_absorbed(sensor.expose(img, noise=False))
+    assert torch.allclose(back, img, rtol=1e-6, atol=0)
 
 
 @pytest.mark.gpu
