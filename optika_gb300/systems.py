@@ -12,6 +12,7 @@ through the extents of the field and pupil stops, which the stop solver
 from __future__ import annotations
 
 import dataclasses
+import functools
 from typing import Sequence
 
 import numpy as np
@@ -169,6 +170,13 @@ class SequentialSystem:
         )
         res.inputs = ObjectVectorArray(wavelength=wl, field=fld, pupil=pup)
         return res
+
+    @functools.cached_property
+    def rayfunction_default(self) -> RayFunctionArray:
+        """:meth:`rayfunction` of :attr:`grid_input`, cached
+        (optika/systems/_sequential.py:990-1000); ``del
+        system.rayfunction_default`` recomputes it."""
+        return self.rayfunction()
 
     def rayfunction(
         self,

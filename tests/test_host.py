@@ -103,6 +103,13 @@ def test_normalized_coordinates_need_stops():
         s.raytrace()
 
 
+def test_rayfunction_default_is_cached_and_needs_stops():
+    s = configs.newtonian()
+    with pytest.raises(ValueError, match="not defined"):
+        s.rayfunction_default
+    assert "rayfunction_default" not in s.__dict__  # nothing cached after a failure
+
+
 def test_configs_are_seeded():
     a = configs.precision_grid(1000)
     b = configs.precision_grid(1000)
