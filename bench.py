@@ -11,11 +11,17 @@ position, direction, intensity, OPL and mask in the sensor frame, plus the
 count and flux images.  Metric: rays*surfaces/s.
 
 ``value`` times the kernel with inputs resident in HBM; ``e2e`` times the
-public ``SequentialSystem.rayfunction`` call from pinned host arrays with the
-host->device input copy and the device->host copy of every output and image
-inside the timed region (the call streams the rays through the GPU in
-chunks whose copies and traces overlap).  ``--impl reference`` times the CPU path (the float64 NumPy
-restatement of the reference's trace, all host cores) on a bounded sample.
+public ``SequentialSystem.rayfunction`` call from pinned host arrays, whose
+zero-copy launch reads the inputs and writes every output over NVLink-C2C
+inside the timed region, with the images copied to the host.
+``--impl reference`` times the CPU path (the float64 NumPy restatement of
+the reference's trace, all host cores) on a bounded sample.
+
+The same line carries ``error``: every output of the first 1e6 of the
+timed rays against the float64 oracle (the exact solution of the
+reference's equations, and the reference's closed forms as written), and
+``workloads``: the batched, multilayer and learned forms at their
+configured sizes (``--workload <name>`` runs one of them alone).
 
 Multi-GPU: rays are independent, so each rank traces its own 1e8 rays with
 no collective on the data path (weak scaling); value = all ranks' work over
@@ -42,11 +48,15 @@ METRIC = "rays*surfaces/s (fused FP32 sequential raytrace, precision form)"
 UNIT = "rays*surfaces/s"
 NUM_SURFACES = 5
 
-# Algorithmic cost of one ray of this workload (counted from the device code
-# path: object, obscuration, coated primary, coated fold, sensor), see the
-# design notes.  Bytes: read 5 x 4 B inputs; write 6 x 4 B position and
-# direction, 4 B intensity, 8 B OPL, 1 B mask.
+# Algorithmic bytes of one ray of this workload: the kernel reads the five
+# float32 inputs (wavelength, field x/y, pupil x/y: 20 B) and writes the
+# float32 position and direction (24 B), float32 intensity (4 B), float64
+# optical path length (8 B) and the uint8 mask (1 B); the sensor images
+# (8 MB) are L2-resident atomics.  Its algorithmic arithmetic per ray is
+# counted by oracle/flops.py over the reference's own formulas (non-trivial
+# real operations only) and frozen in profiles/trace_precision_1e8.json.
 BYTES_PER_RAY = 5 * 4 + 6 * 4 + 4 + 8 + 1
+ERROR_RAYS = 1_000_000
 
 
 def _cpu_worker(args):
@@ -63,6 +73,71 @@ def _cpu_worker(args):
                       g["pupil_y"])
     O.collect(system.sensor, r)
     return n, time.perf_counter() - t0
+
+
+def _error_worker(args):
+    """Oracle outputs of one interleaved chunk of the error sample."""
+    grid, exact = args
+    sys.path.insert(0, str(ROOT))
+    from optika_gb300 import configs
+    from oracle import trace as O
+
+    system = configs.newtonian(coated=True)
+    r = O.rayfunction(system, grid["wavelength"], grid["field_x"], grid["field_y"],
+                      grid["pupil_x"], grid["pupil_y"], exact=exact)
+    return {k: r[k] for k in ("px", "py", "dx", "dy", "dz", "intensity", "opl", "unvignetted")}
+
+
+def precision_errors(grid: dict, out: dict, cores: int) -> dict:
+    """Per-output errors of the GPU's rays ``out`` against the float64
+    oracle on the same (float32) inputs ``grid``: the exact solution of the
+    reference's equations and, for position, its closed forms as written."""
+    import concurrent.futures
+    import multiprocessing as mp
+
+    from optika_gb300 import configs
+    from oracle import trace as O
+
+    n = len(grid["wavelength"])
+    parts = [{k: v[i::cores] for k, v in grid.items()} for i in range(cores)]
+    refs = {}
+    ctx = mp.get_context("spawn")
+    with concurrent.futures.ProcessPoolExecutor(max_workers=cores, mp_context=ctx) as ex:
+        for exact in (True, False):
+            res = list(ex.map(_error_worker, [(p, exact) for p in parts]))
+            ref = {}
+            for k in res[0]:
+                a = np.empty(n, res[0][k].dtype)
+                for i in range(cores):
+                    a[i::cores] = res[i][k]
+                ref[k] = a
+            refs[exact] = ref
+    ex_, lit = refs[True], refs[False]
+    m = ex_["unvignetted"]
+    pix = 0.0135
+    e = np.hypot(out["px"][m] - ex_["px"][m], out["py"][m] - ex_["py"][m])
+    e_lit = np.hypot(out["px"][m] - lit["px"][m], out["py"][m] - lit["py"][m])
+    d_opl = np.abs(out["opl"][m] - ex_["opl"][m])
+    ex_edges, ey_edges = O.histogram_edges(configs.newtonian(coated=True).sensor)
+    fx = (ex_["px"][m] - ex_edges[0]) / pix
+    fy = (ex_["py"][m] - ey_edges[0]) / pix
+    far = (np.abs(fx - np.round(fx)) > 1e-3) & (np.abs(fy - np.round(fy)) > 1e-3)
+    pix_mis = np.count_nonzero(
+        (O.bin_index(ex_edges, out["px"][m][far]) != O.bin_index(ex_edges, ex_["px"][m][far]))
+        | (O.bin_index(ey_edges, out["py"][m][far]) != O.bin_index(ey_edges, ex_["py"][m][far])))
+    return {
+        "rays": n, "reference": "float64 oracle, exact solution of the reference's equations",
+        "mask_mismatches": int(np.count_nonzero(out["unvignetted"] != m)),
+        "position_max_mm": float(e.max()), "position_max_px": float(e.max() / pix),
+        "position_rms_mm": float(np.sqrt(np.mean(e**2))),
+        "position_max_mm_vs_literal_formulas": float(e_lit.max()),
+        "pixel_mismatches_beyond_1e-3_px_of_an_edge": int(pix_mis),
+        "direction_max": float(max(np.abs(out[k][m] - ex_[k][m]).max()
+                                   for k in ("dx", "dy", "dz"))),
+        "opl_max_mm": float(d_opl.max()), "opl_rms_mm": float(np.sqrt(np.mean(d_opl**2))),
+        "intensity_rel_max": float((np.abs(out["intensity"][m] - ex_["intensity"][m])
+                                    / ex_["intensity"][m]).max()),
+    }
 
 
 def cpu_baseline(total_rays: int, cores: int) -> tuple[float, float]:
@@ -91,11 +166,15 @@ class Clocks:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_bench_{index}.csv"
+        self.path = None
 
     def start(self):
+        import tempfile
+
         try:
-            self.path.parent.mkdir(exist_ok=True)
+            fd, name = tempfile.mkstemp(prefix=f"optika_clocks_{self.index}_", suffix=".csv")
+            os.close(fd)
+            self.path = pathlib.Path(name)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
@@ -116,7 +195,9 @@ class Clocks:
         self.f.close()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.path.read_text().splitlines():
+        text = self.path.read_text()
+        self.path.unlink(missing_ok=True)
+        for line in text.splitlines():
             p = [x.strip() for x in line.split(",")]
             if len(p) < 9:
                 continue
@@ -177,7 +258,7 @@ def run_reference(args, rank: int, world: int) -> None:
     print(json.dumps(line), flush=True)
 
 
-def run_surrogate(args, rank: int, world: int) -> None:
+def run_surrogate(args, rank: int, world: int, emit: bool = True) -> dict:
     """The learned form: a 9-256x4-3 BF16 MLP surrogate of the batched
     spectrograph's ray map over 64 configurations, trained on 5e7 rays the
     plain batched kernel traces, evaluated on 1e6 held-out rays, then used to
@@ -279,8 +360,9 @@ def run_surrogate(args, rank: int, world: int) -> None:
         "training": {"steps": args.train_steps, "batch": 65536, "seconds": t_train,
                      "fit_seconds": t_fit, "last": hist[-1]},
     }
-    if rank == 0:
+    if emit and rank == 0:
         print(json.dumps(line), flush=True)
+    return line
 
 
 _BATCH_PARAMS = None
@@ -321,7 +403,7 @@ def _cpu_pool(worker, jobs, cores):
     return sum(r[0] for r in res), wall
 
 
-def run_batched(args, rank: int, world: int) -> None:
+def run_batched(args, rank: int, world: int, emit: bool = True) -> dict:
     """The batched form: 4096 spectrograph configurations (spherical primary,
     toroidal VLS grating, 2048 x 1024 sensor), log-uniform 1e3-1e6 rays each,
     generated on the device and traced in one persistent launch with
@@ -369,8 +451,7 @@ def run_batched(args, rank: int, world: int) -> None:
         n, wall = _cpu_pool(_cpu_batched_worker, jobs, cores)
         cpu = {"value": n * surfaces / wall, "unit": "rays*surfaces/s", "cores": cores,
                "kind": "port", "sample": f"{len(jobs)} configurations x 400000 rays ({wall:.1f} s)"}
-    if rank == 0:
-        print(json.dumps({
+    line = {
             "metric": "rays*surfaces/s (batched spectrograph configurations, one persistent "
                       "launch)",
             "value": value, "unit": "rays*surfaces/s", "n_gpus": world, "steps": args.steps,
@@ -388,7 +469,10 @@ def run_batched(args, rank: int, world: int) -> None:
                          "note": "compute-bound (FP32 issue): the byte roofline is shown for "
                                  "completeness"},
             "cpu_baseline": cpu, "gpu_launches": 3, "clocks": clk,
-        }), flush=True)
+    }
+    if emit and rank == 0:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 def _cpu_multilayer_worker(args):
@@ -430,7 +514,7 @@ def _mirrors(seed: int, count: int):
     return out
 
 
-def run_multilayer(args, rank: int, world: int) -> None:
+def run_multilayer(args, rank: int, world: int, emit: bool = True) -> dict:
     """The multilayer form: 256 periodic 40-bilayer mirrors, 1e7 samples
     (wavelength U(12, 15) nm, incidence U(0, 20) deg, a mirror each), R and
     T for s and p from float-float transfer matrices.  Inputs resident in
@@ -482,8 +566,7 @@ def run_multilayer(args, rank: int, world: int) -> None:
         m, wall = _cpu_pool(_cpu_multilayer_worker, jobs, cores)
         cpu = {"value": m / wall, "unit": "samples/s (s and p)", "cores": cores, "kind": "port",
                "sample": f"{len(jobs)} mirrors x 30000 samples, complex128 ({wall:.1f} s)"}
-    if rank == 0:
-        print(json.dumps({
+    line = {
             "metric": "multilayer samples/s (R and T, s and p, 40-bilayer periodic mirrors)",
             "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -498,7 +581,10 @@ def run_multilayer(args, rank: int, world: int) -> None:
                          "note": "compute-bound (FP32 issue): the byte roofline is shown for "
                                  "completeness"},
             "cpu_baseline": cpu, "gpu_launches": args.steps, "clocks": clk,
-        }), flush=True)
+    }
+    if emit and rank == 0:
+        print(json.dumps(line), flush=True)
+    return line
 
 
 _IMAGE_SURFACES = 5  # object, obscuration, primary, fold, sensor
@@ -719,6 +805,8 @@ def main() -> None:
     ap.add_argument("--ref-rays", type=int, default=2_000_000,
                     help="rays per step of the reference (CPU) arm")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="time the precision form only (no batched, multilayer, surrogate)")
     ap.add_argument("--workload", default="precision",
                     choices=["precision", "surrogate", "batched", "multilayer", "image",
                              "stops"])
@@ -872,32 +960,66 @@ def main() -> None:
         "kernel_ms": kernel_ms,
         "bytes_per_ray": BYTES_PER_RAY,
     }
-    # per-ray DRAM traffic and FP32 operation counts of this kernel, from one
-    # ncu capture of the same workload at 8e6 rays (scaled by the ray count)
+    # per-ray DRAM traffic of this kernel from one ncu capture of the same
+    # workload at 8e6 rays (scaled by the ray count), and the algorithmic
+    # arithmetic per ray counted by oracle/flops.py
     prof = ROOT / "profiles" / "trace_precision_1e8.json"
     if prof.exists():
         pj = json.loads(prof.read_text())
         if pj.get("dram_bytes_per_ray"):
             roofline["traffic"] = pj["dram_bytes_per_ray"] * n
-        if pj.get("flops_per_ray"):
-            # the kernel is bound by FP32 instruction issue, not by HBM: its
-            # FP32 rate against the FP32 pipe's peak at the maximum SM clock
-            # (152 SMs x 128 lanes x 2 flops per FMA; nominal, not measured)
-            fl = pj["flops_per_ray"]
+        if pj.get("algorithmic_flops_per_ray"):
+            # the kernel is bound by FP32 instruction issue, not by HBM: the
+            # reference algorithm's FP32 work per ray at the kernel's rate,
+            # against the FP32 pipe's peak at the maximum SM clock (152 SMs x
+            # 128 lanes x 2 flops per FMA; nominal, no measured FP32 peak
+            # exists for this pool); divisions and special functions are
+            # listed beside it, not added to it
+            fl = pj["algorithmic_flops_per_ray"]
             fp32_peak = 152 * 128 * 2 * float(pk.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
             ach = fl * n / (kernel_ms * 1e-3) / 1e12
-            roofline["fp32"] = {"achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s",
-                                "frac": ach / fp32_peak, "flops_per_ray": fl,
-                                "peak_kind": "nominal at the measured maximum SM clock",
-                                "fma_pipe_active_pct_ncu": pj.get("fma_pipe_active_pct")}
+            roofline["fp32"] = {
+                "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                "algorithmic_flops_per_ray": fl,
+                "algorithmic_div_per_ray": pj.get("algorithmic_div_per_ray"),
+                "algorithmic_special_per_ray": pj.get("algorithmic_special_per_ray"),
+                "counted_by": "oracle/flops.py (non-trivial real operations of the "
+                              "reference's formulas)",
+                "peak_kind": "nominal at the measured maximum SM clock",
+                "executed_fp32_flops_per_ray_ncu": pj.get("flops_per_ray"),
+                "fma_pipe_active_pct_ncu": pj.get("fma_pipe_active_pct")}
 
     cpu = None
+    errors = None
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
         v, wall = cpu_baseline(args.cpu_rays, cores)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{args.cpu_rays} rays of the same workload over {cores} processes "
                          f"({wall:.1f} s)"}
+        # the oracle as the checker of the timed run's first rays
+        k = min(ERROR_RAYS, n)
+        sub = {key: host[key][:k].numpy().astype(np.float64) for key in g}
+        got = {key: prep.bufs[key][:k].cpu().numpy() for key in
+               ("px", "py", "dx", "dy", "dz", "intensity", "opl", "unvignetted")}
+        got["unvignetted"] = got["unvignetted"] != 0
+        errors = precision_errors(sub, got, cores)
+
+    workloads = None
+    if not args.no_workloads:
+        del prep, inp
+        torch.cuda.empty_cache()
+        sub_args = argparse.Namespace(**vars(args))
+        sub_args.steps = min(args.steps, 20)
+        workloads = {}
+        for name, fn in (("batched", run_batched), ("multilayer", run_multilayer),
+                         ("surrogate", run_surrogate)):
+            w = fn(sub_args, rank, world, emit=False)
+            keep = ("metric", "value", "unit", "ms_per_step", "dtype", "config", "roofline",
+                    "cpu_baseline", "gpu_launches", "clocks", "plain_trace", "surrogate_ms",
+                    "speedup_vs_plain", "held_out", "image")
+            workloads[name] = {key: w[key] for key in keep if key in w}
+            torch.cuda.empty_cache()
 
     if rank == 0:
         line = {
@@ -924,8 +1046,10 @@ def main() -> None:
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "ms_per_step": e2e_ms_step,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "error": errors,
             "gpu_launches": args.steps,
             "clocks": clk,
+            "workloads": workloads,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -73,9 +73,9 @@ __global__ void k_sag(const __grid_constant__ otx_system sys, const int mode,
       const float uy = reinterpret_cast<const float*>(in.dy)[i];
       const float uz = reinterpret_cast<const float*>(in.dz)[i];
       const float lo[3] = {0.f, 0.f, 0.f};
-      float px, py, pz;
+      float px, py, pz, tl;
       intercept(s.sag_type, s, sys.newton_iterations, x, y, z0, lo, ux, uy, uz, 0.f, 0.f, 0.f,
-                px, py, pz);
+                px, py, pz, tl);
       reinterpret_cast<float*>(out.px)[i] = px;
       reinterpret_cast<float*>(out.py)[i] = py;
       reinterpret_cast<float*>(out.pz)[i] = pz;

@@ -40,15 +40,47 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-// opl += n t with the product split exactly by an FMA (Dekker's TwoProduct)
-// and the sum by TwoSum; the low parts are gathered in opl_lo.
-__device__ __forceinline__ void opl_add(Ray& r, float n, float t) {
+// |d|^2 - 1 of a near-unit float-float vector d = (x, y, z) + (lx, ly, lz),
+// accurate to ~1e-14: the squares split exactly by FMA (TwoProduct), their
+// sum by TwoSum (Ogita-Rump-Oishi Sum2); s2 is within [0.5, 2], so s2 - 1
+// is exact (Sterbenz).
+__device__ __forceinline__ float norm2_minus_one(float x, float y, float z, float lx, float ly,
+                                                 float lz) {
+  const float p1 = x * x, e1 = fmaf(x, x, -p1);
+  const float p2 = y * y, e2 = fmaf(y, y, -p2);
+  const float p3 = z * z, e3 = fmaf(z, z, -p3);
+  float s, t1, s2, t2;
+  two_sum(p1, p2, s, t1);
+  two_sum(s, p3, s2, t2);
+  const float ld = fmaf(x, lx, fmaf(y, ly, z * lz));
+  return (s2 - 1.f) + fmaf(2.f, ld, (t1 + t2) + (e1 + e2 + e3));
+}
+
+// Make a float-float direction unit to ~1e-14 by moving its low parts
+// (d -> d (1 - e / 2), e = |d|^2 - 1); FP32 rounding leaves |e| ~ 1e-7,
+// which a 400 mm segment would turn into 4e-5 mm of optical path.  Vectors
+// farther from unit length (|e| >= 1e-4: caller-supplied non-unit
+// directions) are left as they are.
+__device__ __forceinline__ void unit_ff(float x, float y, float z, float& lx, float& ly,
+                                        float& lz) {
+  const float e = norm2_minus_one(x, y, z, lx, ly, lz);
+  if (!(fabsf(e) < 1e-4f)) return;
+  const float h = -0.5f * e;
+  lx = fmaf(h, x, lx);
+  ly = fmaf(h, y, ly);
+  lz = fmaf(h, z, lz);
+}
+
+// opl += n (t + tl) for a segment parameter held as a float-float pair:
+// the product n t split exactly by an FMA (Dekker's TwoProduct), the sum by
+// TwoSum; the low parts, with n tl, are gathered in opl_lo.
+__device__ __forceinline__ void opl_add(Ray& r, float n, float t, float tl) {
   const float p = n * t;
   const float pe = fmaf(n, t, -p);
   float s, e;
   two_sum(r.opl_hi, p, s, e);
   r.opl_hi = s;
-  r.opl_lo += e + pe;
+  r.opl_lo += fmaf(n, tl, e + pe);
 }
 
 __device__ __forceinline__ float sgnf(float x) {  // numpy.sign: 0 at 0
@@ -234,12 +266,18 @@ __device__ __forceinline__ float newton_step(int sag_type, const otx_surface& s,
 //
 // The direction's low parts (lx, ly, lz) enter only the intercept point
 // (o_hi + t u_hi) + (o_lo + t u_lo), where they act over the full segment.
+//
+// The segment parameter is returned as a float-float pair t + tl: t is the
+// FP32 value from which the point o + t u is formed (in small coordinates,
+// so that point is accurate), and tl the Newton corrections applied to that
+// point afterwards.  A rounded FP32 t alone would carry up to half an ulp of
+// a ~400 mm segment (1.5e-5 mm) into the optical path length.
 __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
                                            int newton_max, float ox, float oy,
                                            float oz, const float lo[3],
                                            float ux, float uy, float uz,
                                            float lx, float ly, float lz,
-                                           float& x, float& y, float& z) {
+                                           float& x, float& y, float& z, float& tl) {
   const float oxf = ox + lo[0], oyf = oy + lo[1], ozf = oz + lo[2];
   if (sag_type == OTX_SAG_FLAT) {
     const float inv = 1.f / uz;
@@ -252,7 +290,8 @@ __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
     x = fmaf(-dt, ux, x);
     y = fmaf(-dt, uy, y);
     z = 0.f;
-    return t - dt;
+    tl = -dt;
+    return t;
   }
   float t;
   bool polish = true;
@@ -353,12 +392,16 @@ __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
   x = fmaf(t, ux, ox) + fmaf(t, lx, lo[0]);
   y = fmaf(t, uy, oy) + fmaf(t, ly, lo[1]);
   z = fmaf(t, uz, oz) + fmaf(t, lz, lo[2]);
+  tl = 0.f;
   if (sag_type == OTX_SAG_TOROID) {
     const int iters = newton_max > 0 ? newton_max : 12;
     bool conv = false;
     for (int i = 0; i < iters; ++i) {
       const float dt = newton_step(sag_type, s, x, y, z, ux, uy, uz);
-      t -= dt;
+      float ts, te;
+      two_sum(t, -dt, ts, te);
+      t = ts;
+      tl += te;
       if (fabsf(dt) <= 1e-7f * (1.f + fabsf(t))) {
         conv = true;
         break;
@@ -368,7 +411,7 @@ __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
       x = y = z = NAN;
     }
   } else if (polish && isfinite(t)) {
-    t -= newton_step(sag_type, s, x, y, z, ux, uy, uz);
+    tl = -newton_step(sag_type, s, x, y, z, ux, uy, uz);
   }
   return t;
 }
@@ -525,8 +568,11 @@ __device__ __forceinline__ void snell(float& ax, float& ay, float& az, float& lx
   az = r * bz;
   // The formula's b is unit in exact arithmetic for any a (|b|^2 =
   // r^2 (|a|^2 + 2 d a.u + d^2) = 1); renormalising removes a residue
-  // along the normal beyond FP32 rounding.
+  // along the normal beyond FP32 rounding, and the low parts then take
+  // up what FP32 rounding left (the mirror path with a unit direction and
+  // a flat sag's exact normal preserves the norm and skips this).
   normalize3(ax, ay, az, lx, ly, lz);
+  if (!(mirror && unit && n1 == n2)) unit_ff(ax, ay, az, lx, ly, lz);
 }
 
 // Reflection off a curved mirror, b = a - 2 (a.v) v / (v.v), with v parallel
@@ -1253,9 +1299,9 @@ __device__ __forceinline__ void propagate_surface(const otx_system& sys,
   const float ox = r.px, oy = r.py, oz = r.pz;
 
   // sag.propagate_rays (sags/_abc.py:109-122)
-  float x, y, z;
+  float x, y, z, tl;
   const float t = intercept(sag_type, s, sys.newton_iterations, ox, oy, oz, lo, r.dx,
-                            r.dy, r.dz, r.lx, r.ly, r.lz, x, y, z);
+                            r.dy, r.dz, r.lx, r.ly, r.lz, x, y, z, tl);
   r.px = x;
   r.py = y;
   r.pz = z;
@@ -1263,7 +1309,10 @@ __device__ __forceinline__ void propagate_surface(const otx_system& sys,
     const float len = fabsf(t) * sqrtf(r.dx * r.dx + r.dy * r.dy + r.dz * r.dz);
     r.inten *= expf(-r.att * len);
   }
-  opl_add(r, r.n, t);
+  // (t + tl) is the segment's geometric length: directions are unit to
+  // float-float accuracy (unit_ff at their creation and after refraction;
+  // rotations and reflections preserve the norm).
+  opl_add(r, r.n, t, tl);
 
   float nx, ny, nz, v[3];
   normal(sag_type, s, x, y, nx, ny, nz, v);

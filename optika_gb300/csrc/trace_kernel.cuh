@@ -36,6 +36,7 @@ __device__ __forceinline__ void load_ray(const TraceArgs& a, int64_t i, Ray& r) 
     r.dy = reinterpret_cast<const float*>(in.dy)[i];
     r.dz = reinterpret_cast<const float*>(in.dz)[i];
     r.lx = r.ly = r.lz = 0.f;
+    unit_ff(r.dx, r.dy, r.dz, r.lx, r.ly, r.lz);
     r.wl = in.wavelength ? reinterpret_cast<const float*>(in.wavelength)[i] : 0.f;
     r.inten = in.intensity ? reinterpret_cast<const float*>(in.intensity)[i] : 1.f;
     r.att = in.attenuation ? reinterpret_cast<const float*>(in.attenuation)[i] : 0.f;
@@ -62,6 +63,7 @@ __device__ __forceinline__ void load_ray(const TraceArgs& a, int64_t i, Ray& r) 
     }
     r.pz = 0.f;
     r.lx = r.ly = r.lz = 0.f;
+    unit_ff(r.dx, r.dy, r.dz, r.lx, r.ly, r.lz);
     r.wl = wl;
     r.inten = g.intensity ? reinterpret_cast<const float*>(g.intensity)[i * g.stride_intensity] : 1.f;
     r.att = 0.f;

@@ -138,8 +138,34 @@ def sag_normal(sag, x, y):
     return gx / L, gy / L, -1 / L
 
 
-def sag_intercept(sag, o, u, newton_tol=1e-12, newton_max=60):
+def _polish_root(sag, o, u, t, iters=3, reach=1e-3):
+    """Float64 Newton steps on f(t) = z(t) - sag(x(t), y(t)) from the
+    reference formula's root ``t``: the same root (the same sheet and
+    branch), free of the cancellation of that formula.  Only points within
+    ``reach`` mm of the sag are moved; others keep ``t``."""
+    ox, oy, oz = o
+    ux, uy, uz = u
+    with np.errstate(all="ignore"):
+        x, y, z = ox + ux * t, oy + uy * t, oz + uz * t
+        near = np.isfinite(t) & (np.abs(z - sag_value(sag, x, y)) < reach)
+        for _ in range(iters):
+            x, y, z = ox + ux * t, oy + uy * t, oz + uz * t
+            nx, ny, nz = sag_normal(sag, x, y)
+            gx, gy = -nx / nz, -ny / nz
+            dt = (z - sag_value(sag, x, y)) / (uz - gx * ux - gy * uy)
+            t = np.where(near & np.isfinite(dt), t - dt, t)
+    return t
+
+
+def sag_intercept(sag, o, u, newton_tol=1e-12, newton_max=60, exact=False):
     """Line parameter t of the intercept of rays o + t u.
+
+    ``exact=False`` evaluates the reference's closed forms literally, with
+    their float64 rounding: the conic's ``(-B +- sqrt(B^2 - 4AC)) / 2A``
+    loses up to ~1e-4 mm along a near-axial ray (A ~ 1e-12 / mm), which is
+    the reference's own error.  ``exact=True`` keeps the root those forms
+    choose and polishes it with float64 Newton steps on the sag equation
+    (:func:`_polish_root`): the float64 solution of the same problem.
 
     flat      _flat.py:47-64
     sphere    _spherical.py:148-191
@@ -149,6 +175,14 @@ def sag_intercept(sag, o, u, newton_tol=1e-12, newton_max=60):
               plane intercept, iterated to convergence in float64)
     cylinder  _cylindrical.py:115-160
     """
+    t = _sag_intercept_literal(sag, o, u, newton_tol, newton_max)
+    if exact and _sag_kind(sag) in ("SphericalSag", "ConicSag", "ParabolicSag",
+                                    "CylindricalSag"):
+        t = _polish_root(sag, o, u, t)
+    return t
+
+
+def _sag_intercept_literal(sag, o, u, newton_tol, newton_max):
     ox, oy, oz = o
     ux, uy, uz = u
     k = _sag_kind(sag)
@@ -441,7 +475,7 @@ def layer_index(chemical, wavelength):
     """Complex index of a layer medium: vacuum, constant, or a table
     interpolated linearly with the ends held (optika/chemicals/_chemicals.py:
     101-144; numpy.interp semantics for na.interp)."""
-    w = np.asarray(wavelength, dtype=np.float64)
+    w = np.asanyarray(wavelength, dtype=np.float64)
     if chemical is None:
         return np.ones_like(w) + 0j
     if hasattr(chemical, "wavelength"):
@@ -552,10 +586,12 @@ def _sequence_transfer(items, wavelength, cos, n, s, where):
 def multilayer_efficiency(wavelength, direction=1.0, n=1.0, layers=None, substrate=None):
     """(R_s, R_p, T_s, T_p), optika/materials/_multilayers.py:33-237 and
     240-532, in complex128."""
+    # (subclass-preserving conversions: oracle/flops.py counts this code's
+    # arithmetic on a counting array type)
     wavelength, direction, n = np.broadcast_arrays(
-        np.asarray(wavelength, dtype=np.float64),
-        np.asarray(direction, dtype=np.complex128),
-        np.asarray(n, dtype=np.complex128),
+        np.asanyarray(wavelength, dtype=np.float64),
+        np.asanyarray(direction, dtype=np.complex128),
+        np.asanyarray(n, dtype=np.complex128), subok=True,
     )
     items = _flatten(layers)
     sub_chem = None if substrate is None else substrate.chemical
@@ -587,14 +623,15 @@ def _material(mat):
     return name
 
 
-def propagate_surface(surface, rays: dict) -> dict:
-    """optika/surfaces.py:123-198 with rays in the parent frame."""
+def propagate_surface(surface, rays: dict, exact: bool = False) -> dict:
+    """optika/surfaces.py:123-198 with rays in the parent frame (``exact``:
+    see :func:`sag_intercept`)."""
     T = _mat(surface.transformation)
     r = apply(_inv(T), rays)
     sag = surface.sag
     o = (r["px"], r["py"], r["pz"])
     u = (r["dx"], r["dy"], r["dz"])
-    t = sag_intercept(sag, o, u)
+    t = sag_intercept(sag, o, u, exact=exact)
     with np.errstate(all="ignore"):
         px, py, pz = o[0] + u[0] * t, o[1] + u[1] * t, o[2] + u[2] * t
         disp = np.sqrt((px - o[0]) ** 2 + (py - o[1]) ** 2 + (pz - o[2]) ** 2)
@@ -697,29 +734,30 @@ def input_rays(system, wavelength, field_x, field_y, pupil_x, pupil_y, intensity
 
 
 def raytrace(system, wavelength, field_x, field_y, pupil_x, pupil_y, intensity=None,
-             accumulate=True):
+             accumulate=True, exact=False):
     """optika/systems/_sequential.py:836-925: list of rays after every
     surface (accumulate) or the last rays, in the system frame."""
     rays = input_rays(system, wavelength, field_x, field_y, pupil_x, pupil_y, intensity)
     out = []
     for s in system.surfaces_all:
-        rays = propagate_surface(s, rays)
+        rays = propagate_surface(s, rays, exact=exact)
         out.append(rays)
     return out if accumulate else rays
 
 
-def rayfunction(system, wavelength, field_x, field_y, pupil_x, pupil_y, intensity=None):
+def rayfunction(system, wavelength, field_x, field_y, pupil_x, pupil_y, intensity=None,
+                exact=False):
     """optika/systems/_sequential.py:927-988: last rays in the sensor frame."""
     rays = raytrace(system, wavelength, field_x, field_y, pupil_x, pupil_y, intensity,
-                    accumulate=False)
+                    accumulate=False, exact=exact)
     return apply(_inv(_mat(system.sensor.transformation)), rays)
 
 
-def propagate_rays(surfaces, rays: dict, accumulate=False):
+def propagate_rays(surfaces, rays: dict, accumulate=False, exact=False):
     """optika/propagators.py:19-73."""
     out = []
     for s in surfaces:
-        rays = propagate_surface(s, rays)
+        rays = propagate_surface(s, rays, exact=exact)
         out.append(rays)
     return out if accumulate else rays
 

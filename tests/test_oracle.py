@@ -185,6 +185,44 @@ def test_cylinder_known_answers():
     assert np.allclose(t, 10.0)
 
 
+@pytest.mark.parametrize("sag", _sags(), ids=lambda s: type(s).__name__)
+def test_exact_intercept_keeps_the_reference_root(sag):
+    """The exact mode polishes the root the reference's closed form picks:
+    the same root to the literal form's rounding, on the sag to float64
+    rounding."""
+    o, u = _rays()
+    t_lit = O.sag_intercept(sag, o, u)
+    t_ex = O.sag_intercept(sag, o, u, exact=True)
+    assert np.allclose(t_ex, t_lit, rtol=0, atol=1e-7)
+    x, y, z = (o[i] + u[i] * t_ex for i in range(3))
+    assert np.abs(O.sag_value(sag, x, y) - z).max() < 1e-12
+
+
+def test_literal_conic_intercept_cancels_for_near_axial_rays():
+    """The reference's (-B +- sqrt(B^2 - 4 A C)) / 2A (optika/sags/_conic.py:
+    144-162) loses float64 digits when A = c (u_x^2 + u_y^2) is small but
+    above the 1e-12 linear-branch threshold: the Newtonian primary
+    (R -800 mm, k -1) with field angles of ~3e-5 rad.  The exact mode's
+    point lies on the sag; the literal one can be ~1e-4 mm off it."""
+    sag = ok.sags.ConicSag(radius=-800.0, conic=-1.0)
+    rng = np.random.default_rng(12)
+    n = 2000
+    ang = rng.uniform(2.9e-5, 4e-5, n)
+    phi = rng.uniform(0, 2 * np.pi, n)
+    u = O.direction(ang * np.cos(phi), ang * np.sin(phi))
+    r = np.sqrt(rng.uniform(12**2, 50**2, n))
+    o = (r * np.cos(phi), r * np.sin(phi), np.full(n, -350.0))
+    c = 1 / sag.radius
+    assert np.all(np.abs(c * (u[0] ** 2 + u[1] ** 2)) > 1e-12)
+    res = {}
+    for exact in (False, True):
+        t = O.sag_intercept(sag, o, u, exact=exact)
+        x, y, z = (o[i] + u[i] * t for i in range(3))
+        res[exact] = np.abs(O.sag_value(sag, x, y) - z)
+    assert res[True].max() < 1e-12
+    assert res[False].max() > 1e-6
+
+
 def test_parabola_equals_conic():
     p = ok.sags.ParabolicSag(focal_length=-120.0)
     c = ok.sags.ConicSag(radius=-240.0, conic=-1.0)

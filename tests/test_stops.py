@@ -125,8 +125,13 @@ def test_gpu_normalized_raytrace(cuda):
                       normalized_field=False, normalized_pupil=False)
     torch.cuda.synchronize()
     oa, ob = a.outputs.numpy(), b.outputs.numpy()
-    m = ob["unvignetted"]
-    assert np.array_equal(oa["unvignetted"], m)
+    # normalised pupil coordinates of +-1 put a ray on the stop's edge by
+    # construction (the solved extents are where rays graze it): the two
+    # sides' extents differ by FP32 rounding, so only rays strictly inside
+    # have a defined mask; every ray unvignetted on both sides must land alike
+    inside = (np.abs(qx) < 1) & (np.abs(qy) < 1)
+    assert np.array_equal(oa["unvignetted"][inside], ob["unvignetted"][inside])
+    m = ob["unvignetted"] & oa["unvignetted"]
     assert np.abs(oa["px"][m] - ob["px"][m]).max() < 1e-4
     assert np.abs(oa["py"][m] - ob["py"][m]).max() < 1e-4
     # the pupil corners reach the stop's edge: some rays are vignetted, not all

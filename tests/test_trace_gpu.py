@@ -452,3 +452,55 @@ def test_multilayer_periodic_batched_vs_oracle(cuda):
         ref = O.multilayer_efficiency(wl[sel], cos[sel], 1.0, m.layers, m.substrate)
         for g, r in zip(got, ref):
             assert np.abs(g[sel] - r).max() < 1e-5
+
+
+def test_attenuation_through_refracting_surface(cuda):
+    """Rays in an absorbing medium (attenuation alpha > 0) lose
+    I exp(-alpha |delta x|) on the way to the first surface
+    (optika/sags/_abc.py:116-120); the glass behind it is clear."""
+    rng = np.random.default_rng(31)
+    r = _single_surface_rays(n=4000, seed=31)
+    r["attenuation"] = rng.uniform(1e-3, 1e-2, r["px"].size).astype(np.float32).astype(np.float64)
+    lens = SURFACES["glass_lens"]
+    det = ok.surfaces.Surface(transformation=ok.transforms.Translation(z=-300.0))
+    ref = O.propagate_rays([lens, det], r)
+    out = _gpu_propagate([lens, det], r)
+    m = ref["unvignetted"] & np.isfinite(ref["px"])
+    assert m.mean() > 0.9
+    # the factor is far from 1: exp(-alpha 100 mm) spans 0.37-0.9
+    assert ref["intensity"][m].min() < 0.5 and ref["intensity"][m].max() > 0.85
+    assert np.allclose(out["intensity"][m], ref["intensity"][m], rtol=2e-6, atol=0)
+    assert np.all(out["attenuation"][m] == 0.0)
+    assert np.abs(out["px"][m] - ref["px"][m]).max() < 2e-4
+
+
+def test_attenuation_into_multilayer_mirror(cuda):
+    """Rays arriving through an absorbing medium at a multilayer mirror: the
+    incident index becomes n + i alpha lambda / (4 pi)
+    (optika/materials/_multilayers.py:927-935), the segment loses
+    exp(-alpha |delta x|), and the mirror keeps the medium's attenuation."""
+    rng = np.random.default_rng(37)
+    n = 4000
+    r = O.make_rays((n,), px=rng.uniform(-1, 1, n), py=rng.uniform(-1, 1, n),
+                    pz=np.full(n, -2e-4))
+    dx, dy, dz = O.direction(rng.uniform(-0.2, 0.2, n), rng.uniform(-0.2, 0.2, n))
+    r.update(dx=dx, dy=dy, dz=dz, wavelength=rng.uniform(12.5, 14.5, n),
+             attenuation=rng.uniform(1000.0, 5000.0, n))
+    for k in ("px", "py", "pz", "dx", "dy", "dz", "wavelength", "attenuation"):
+        r[k] = r[k].astype(np.float32).astype(np.float64)
+    si = ok.materials.Layer(c32(0.999 + 0.0018j), 4.1)
+    mo = ok.materials.Layer(c32(0.922 + 0.0064j), 2.8)
+    mirror = ok.surfaces.Surface(material=ok.materials.MultilayerMirror(
+        layers=ok.materials.PeriodicLayerSequence([si, mo], num_periods=10),
+        substrate=ok.materials.Layer(c32(0.999 + 0.0018j))))
+    ref = O.propagate_rays([mirror], r)
+    out = _gpu_propagate([mirror], r)
+    # the imaginary part alpha lambda / 4 pi (1e-3 - 6e-3) changes R: the
+    # same mirror seen from a clear medium reflects differently
+    clear = dict(r, attenuation=np.zeros(n))
+    ref_clear = O.propagate_rays([mirror], clear)
+    assert np.abs(ref["intensity"] - ref_clear["intensity"]
+                  * np.exp(-r["attenuation"] * 2e-4 / r["dz"])).max() > 1e-3
+    # the multilayer tolerance of the single-precision transfer-matrix product
+    assert np.abs(out["intensity"] - ref["intensity"]).max() < 1e-5
+    assert np.allclose(out["attenuation"], ref["attenuation"], rtol=0, atol=0)
