@@ -35,9 +35,7 @@ __device__ __forceinline__ void batch_ray(const otx_batch& b, int cfg, int64_t i
   r.px = qx;
   r.py = qy;
   r.pz = 0.f;
-  direction_from_angles(fx, fy, r.dx, r.dy, r.dz);
-  r.lx = r.ly = r.lz = 0.f;
-  unit_ff(r.dx, r.dy, r.dz, r.lx, r.ly, r.lz);
+  direction_from_angles(fx, fy, r.dx, r.dy, r.dz, r.lx, r.ly, r.lz);
   r.wl = wl;
   r.inten = 1.f;
   r.att = 0.f;

@@ -193,6 +193,11 @@ __device__ __forceinline__ float sag_eval(int sag_type, const otx_surface& s, fl
       const float c = s.sag_curvature;
       const float kp1 = (sag_type == OTX_SAG_SPHERE) ? 1.f : 1.f + s.sag_conic;
       const float r2 = fmaf(x, x, y * y);
+      if (kp1 == 0.f) {  // paraboloid: g = 1 exactly, the same values below
+        gx = c * x;
+        gy = c * y;
+        return 0.5f * (c * r2);
+      }
       const float g = sqrtf(1.f - kp1 * c * c * r2);
       const float cg = c / g;
       gx = cg * x;
@@ -630,6 +635,50 @@ __device__ __forceinline__ void reflect_curved(float& ax, float& ay, float& az, 
   lx = bl[0];
   ly = bl[1];
   lz = bl[2];
+  normalize3(ax, ay, az, lx, ly, lz);
+}
+
+// Reflection off a curved mirror whose normal is parallel to the gradient
+// form v = (gx, gy, -1) (conic, paraboloid, toroid): reflect_curved with
+// v.v = 1 + (gx^2 + gy^2) and a.v = -a_z + (a_x gx + a_y gy) each formed as
+// a float-float pair around their dominant exact term, and the quotient
+// from one reciprocal with a float-float correction.
+__device__ __forceinline__ void reflect_gradient(float& ax, float& ay, float& az, float& lx,
+                                                 float& ly, float& lz, float gx, float gy) {
+  // a.v
+  float n_hi, n_lo;
+  two_sum(-az, fmaf(ax, gx, ay * gy), n_hi, n_lo);
+  n_lo += fmaf(lx, gx, fmaf(ly, gy, -lz));
+  // v.v = 1 + q, q = gx^2 + gy^2 with the products' errors
+  const float p1 = gx * gx, e1 = fmaf(gx, gx, -p1);
+  const float p2 = gy * gy, e2 = fmaf(gy, gy, -p2);
+  float q, eq;
+  two_sum(p1, p2, q, eq);
+  float d_hi, d_lo;
+  two_sum(1.f, q, d_hi, d_lo);
+  d_lo += eq + (e1 + e2);
+  // k = 2 (a.v) / (v.v) as a float-float pair
+  const float inv = 1.f / d_hi;
+  const float q_hi = n_hi * inv;
+  const float rem = (fmaf(-q_hi, d_hi, n_hi) + n_lo) - q_hi * d_lo;
+  const float k_hi = 2.f * q_hi, k_lo = 2.f * (rem * inv);
+  // b = a - k v: x and y subtract k g, z adds k
+  float s, e;
+  {
+    const float p = k_hi * gx, pe = fmaf(k_hi, gx, -p);
+    two_sum(ax, -p, s, e);
+    ax = s;
+    lx = e + (lx - pe - k_lo * gx);
+  }
+  {
+    const float p = k_hi * gy, pe = fmaf(k_hi, gy, -p);
+    two_sum(ay, -p, s, e);
+    ay = s;
+    ly = e + (ly - pe - k_lo * gy);
+  }
+  two_sum(az, k_hi, s, e);
+  az = s;
+  lz = e + (lz + k_lo);
   normalize3(ax, ay, az, lx, ly, lz);
 }
 
@@ -1224,11 +1273,28 @@ __device__ __forceinline__ bool stack_has_layers(const otx_stack& K) {
 // Substrate-only stack with a smooth substrate (a bare coating, or a film of
 // no layers): the multilayer product reduces to one interface, r = (q0 - q1) / (q0 + q1),
 // t = 2 q0 / (q0 + q1); returns the s/p average of R (mirror) or T.
+//
+// For a mirror both polarisations share n1 cos1 = n1 sqrt(1 - (n0 sin0)^2 /
+// n1^2) (one complex square root): with q0 = n0 cos0 and w = n1 cos1,
+//   R_s = |q0 - w|^2 / |q0 + w|^2,
+//   R_p = |q0 |n1|^2 - w |n0|^2|^2 / |q0 |n1|^2 + w |n0|^2|^2
+// (the p admittances conj(n cos) / |n|^2 scaled by |n0|^2 |n1|^2 and
+// conjugated), and the average (R_s + R_p) / 2 takes one division.
 __device__ __forceinline__ float fresnel_efficiency(const otx_system& sys, const otx_stack& K,
                                                     bool mirror, float wl, float cos0, cf n0) {
   cf n1{1.f, 0.f};
   if (K.substrate >= 0) n1 = layer_n(sys, sys.layers[K.substrate], wl);
   const cf inv0 = cscale(cmul(n0, n0), fmaf(-cos0, cos0, 1.f));
+  if (mirror) {
+    const cf w = medium_q(inv0, n1, false);
+    const cf q0 = cscale(n0, cos0);
+    const float ns = cabs2(csub(q0, w)), ds = cabs2(cadd(q0, w));
+    const cf a = cscale(q0, cabs2(n1)), b = cscale(w, cabs2(n0));
+    const float np = cabs2(csub(a, b)), dp = cabs2(cadd(a, b));
+    const float den = ds * dp;
+    if (den > 1e-30f && den < 1e30f) return 0.5f * __fdividef(fmaf(ns, dp, np * ds), den);
+    return 0.5f * (ns / ds + np / dp);
+  }
   float acc = 0.f;
 #pragma unroll
   for (int p = 0; p < 2; ++p) {
@@ -1236,11 +1302,7 @@ __device__ __forceinline__ float fresnel_efficiency(const otx_system& sys, const
     const cf q0 = pol_p ? cscale(cconj(n0), cos0 / cabs2(n0)) : cscale(n0, cos0);
     const cf q1 = medium_q(inv0, n1, pol_p);
     const float den = cabs2(cadd(q0, q1));
-    if (mirror) {
-      acc += cabs2(csub(q0, q1)) / den;
-    } else {
-      acc += 4.f * cabs2(q0) / den * cdiv(q1, q0).re;
-    }
+    acc += 4.f * cabs2(q0) / den * cdiv(q1, q0).re;
   }
   return 0.5f * acc;
 }
@@ -1373,11 +1435,22 @@ __device__ __forceinline__ void propagate_surface(const otx_system& sys,
                                         r.wl, nx, ny, nz);
   // wavelength_2 = wavelength_1 / (n1 / n2)   (surfaces.py:162-165)
   if (n2 != n1) r.wl = r.wl / (n1 / n2);
-  if (mirror && sag_type != OTX_SAG_FLAT && rule_type == OTX_RULE_NONE &&
-      fabsf(fmaf(r.dx, r.dx, fmaf(r.dy, r.dy, fmaf(r.dz, r.dz, -1.f)))) < 1e-6f)
+  const bool unit_mirror =
+      mirror && rule_type == OTX_RULE_NONE &&
+      fabsf(fmaf(r.dx, r.dx, fmaf(r.dy, r.dy, fmaf(r.dz, r.dz, -1.f)))) < 1e-6f;
+  if (unit_mirror && sag_type == OTX_SAG_FLAT) {
+    // the flat's normal is exactly (0, 0, -1): Snell's mirror case reduces
+    // to negating the z component (the same values, without the dot product)
+    r.dz = -r.dz;
+    r.lz = -r.lz;
+  } else if (unit_mirror && (sag_type == OTX_SAG_CONIC || sag_type == OTX_SAG_PARABOLA ||
+                             sag_type == OTX_SAG_TOROID)) {
+    reflect_gradient(r.dx, r.dy, r.dz, r.lx, r.ly, r.lz, v[0], v[1]);
+  } else if (unit_mirror) {
     reflect_curved(r.dx, r.dy, r.dz, r.lx, r.ly, r.lz, v);
-  else
+  } else {
     snell(r.dx, r.dy, r.dz, r.lx, r.ly, r.lz, n1, n2, mirror, nx, ny, nz);
+  }
   r.inten *= eff;
   r.att = att2;
   r.n = n2;

@@ -13,16 +13,54 @@
 namespace otx {
 
 
-// direction cosines from (azimuth, elevation), optika/_util.py:69-73
-__device__ __forceinline__ void direction_from_angles(float ax, float ay,
-                                                      float& dx, float& dy,
-                                                      float& dz) {
+// sin a as a float-float pair and cos a - 1, for |a| <= 1/16 rad, from
+// their Taylor series (truncation below 1e-12 of the result there):
+//   sin a     = a + a p,  p = a^2 (-1/6 + a^2 (1/120 - a^2 / 5040))
+//   cos a - 1 = a^2 (-1/2 + a^2 (1/24 - a^2 (1/720 - a^2 / 40320)))
+// The high part of sin a is a + a p rounded once; its low part is the
+// rounding error, recovered exactly by an FMA (a - s is exact by Sterbenz).
+__device__ __forceinline__ void sin_cosm1_small(float a, float& s_hi, float& s_lo, float& cm1) {
+  const float a2 = a * a;
+  const float p = a2 * fmaf(a2, fmaf(a2, -1.f / 5040.f, 1.f / 120.f), -1.f / 6.f);
+  s_hi = fmaf(a, p, a);
+  s_lo = fmaf(a, p, a - s_hi);
+  cm1 = a2 * fmaf(a2, fmaf(a2, fmaf(a2, 1.f / 40320.f, -1.f / 720.f), 1.f / 24.f), -0.5f);
+}
+
+// Direction cosines from (azimuth, elevation), optika/_util.py:69-73:
+// (-cos ay sin ax, -sin ay, cos ay cos ax), as a float-float vector unit to
+// ~1e-12.  Angles up to 1/16 rad (every field of the telescopes and
+// spectrographs here) take the series above, with cos written as 1 + (cos - 1)
+// so that the direction's dominant component keeps its low part; larger
+// angles take sincosf and unit_ff.
+__device__ __forceinline__ void direction_from_angles(float ax, float ay, float& dx, float& dy,
+                                                      float& dz, float& lx, float& ly,
+                                                      float& lz) {
+  if (fmaxf(fabsf(ax), fabsf(ay)) <= 0.0625f) {
+    float sxh, sxl, cmx, syh, syl, cmy;
+    sin_cosm1_small(ax, sxh, sxl, cmx);
+    sin_cosm1_small(ay, syh, syl, cmy);
+    // -cos ay sin ax = -(sx + (cos ay - 1) sx)
+    const float xh = fmaf(cmy, sxh, sxh);
+    const float xl = fmaf(cmy, sxh, sxh - xh) + fmaf(cmy, sxl, sxl);
+    dx = -xh;
+    lx = -xl;
+    dy = -syh;
+    ly = -syl;
+    // cos ay cos ax = 1 + s, s = (cos ax - 1) + (cos ay - 1) + (cos ax - 1)(cos ay - 1)
+    const float sz = fmaf(cmx, cmy, cmx + cmy);
+    dz = 1.f + sz;
+    lz = sz - (dz - 1.f);
+    return;
+  }
   float sx, cx, sy, cy;
   sincosf(ax, &sx, &cx);
   sincosf(ay, &sy, &cy);
   dx = -cy * sx;
   dy = -sy;
   dz = cy * cx;
+  lx = ly = lz = 0.f;
+  unit_ff(dx, dy, dz, lx, ly, lz);
 }
 
 template <int MODE>
@@ -55,15 +93,13 @@ __device__ __forceinline__ void load_ray(const TraceArgs& a, int64_t i, Ray& r) 
     if (MODE == OTX_INPUT_GRID_INFINITY) {
       r.px = qx;
       r.py = qy;
-      direction_from_angles(fx, fy, r.dx, r.dy, r.dz);
+      direction_from_angles(fx, fy, r.dx, r.dy, r.dz, r.lx, r.ly, r.lz);
     } else {
       r.px = fx;
       r.py = fy;
-      direction_from_angles(qx, qy, r.dx, r.dy, r.dz);
+      direction_from_angles(qx, qy, r.dx, r.dy, r.dz, r.lx, r.ly, r.lz);
     }
     r.pz = 0.f;
-    r.lx = r.ly = r.lz = 0.f;
-    unit_ff(r.dx, r.dy, r.dz, r.lx, r.ly, r.lz);
     r.wl = wl;
     r.inten = g.intensity ? reinterpret_cast<const float*>(g.intensity)[i * g.stride_intensity] : 1.f;
     r.att = 0.f;
@@ -189,7 +225,24 @@ __device__ __forceinline__ void propagate_fixed(const otx_system& sys, Ray& r) {
   if constexpr (sizeof...(Rest) > 0) propagate_fixed<I + 1, Rest...>(sys, r);
 }
 
-template <int MODE, class... Ks>
+// Whether surface 0 leaves the rays of a grid input unchanged: a flat
+// vacuum surface without aperture or rulings whose frame is the input frame.
+// Grid rays start on its plane (z = 0) in vacuum (n = 1, no attenuation), so
+// its intercept is at t = 0, the Snell step between equal indices keeps the
+// (unit) direction and nothing clips: the step is an exact no-op.
+template <int MODE, class K>
+__device__ __forceinline__ bool first_is_noop(const otx_system& sys) {
+  if constexpr (MODE != OTX_INPUT_RAYS && K::sag == OTX_SAG_FLAT && K::mat == OTX_MAT_VACUUM &&
+                K::aper == OTX_APER_NONE && K::rule == OTX_RULE_NONE) {
+    const otx_affine& f = sys.surfaces[0].to_local;
+    return (f.flags & OTX_AFFINE_ROT_IDENTITY) && f.t_hi[0] == 0.f && f.t_hi[1] == 0.f &&
+           f.t_hi[2] == 0.f && f.t_lo[0] == 0.f && f.t_lo[1] == 0.f && f.t_lo[2] == 0.f;
+  } else {
+    return false;
+  }
+}
+
+template <int MODE, class K0, class... Ks>
 __global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
     k_trace_fixed(const __grid_constant__ otx_system sys,
                   const __grid_constant__ TraceArgs a) {
@@ -197,10 +250,12 @@ __global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
   const int64_t step = (int64_t)gridDim.x * blockDim.x;
   const bool bin = image_any(a.img);
   const bool final_identity = (sys.flags & OTX_SYS_FLAG_FINAL_IDENTITY) != 0;
+  const bool skip0 = first_is_noop<MODE, K0>(sys);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
     Ray r;
     load_ray<MODE>(a, i, r);
-    propagate_fixed<0, Ks...>(sys, r);
+    if (!skip0) propagate_surface<K0, false>(sys, sys.surfaces[0], r);
+    if constexpr (sizeof...(Ks) > 0) propagate_fixed<1, Ks...>(sys, r);
     if (bin) bin_ray(sys.sensor, a.img, r);
     if (final_identity)
       store_ray<true>(a.out, i, sys.final_to_output, r);
