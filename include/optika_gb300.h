@@ -421,12 +421,16 @@ otx_status otx_trace_batch(const otx_system* base, const otx_batch* batch,
  * library whose device memory belongs to its own allocator, or code that
  * may not allocate (allocation synchronises the device).  They pass only
  * the inputs and outputs of otx_trace_batch; batch->tiles and
- * batch->counter are ignored, batch->num_tiles must equal
- * sum over configs of ceil(rays / tile_size) and may not exceed
- * OTX_NOALLOC_MAX_TILES (larger batches return OTX_ERR_SIZE).  The work
- * counter and the tile list live in a file-scope device array of the
- * library (1 MiB, held by every GPU that loads the library until exit); the
- * first call on a device looks up its address, so make it before any stream
+ * batch->counter are ignored.  The library builds the tile list itself
+ * from batch->ray_offset; batch->num_tiles, the caller's count of work
+ * items (sum over configs of ceil(rays / tile_size)), may not exceed
+ * OTX_NOALLOC_MAX_TILES (OTX_ERR_SIZE), and work items beyond that
+ * capacity are never traced.  Each configuration holds at most 2^31 - 1
+ * rays (a larger one is not traced).  The work counter and the tile list
+ * live in a file-scope device array of the library (1 MiB, held by every
+ * GPU that loads the library until exit), whose address on the current
+ * device every call looks up (no allocation); the first call on a device
+ * also loads the library's kernels there, so make it before any stream
  * capture.  Every call shares that array and keeps the last call's
  * contents: calls that overlap on the GPU (on concurrent streams) race. */
 #define OTX_NOALLOC_MAX_TILES 131000

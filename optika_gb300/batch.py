@@ -87,6 +87,9 @@ class BatchedTrace:
         counts = np.asarray(ray_counts, dtype=np.int64)
         if counts.shape != (n_cfg,) or np.any(counts < 0):
             raise ValueError("ray_counts must give one non-negative count per configuration")
+        if np.any(counts > np.iinfo(np.int32).max):
+            # a work item stores its first ray as int32 (otx_batch.tiles)
+            raise ValueError("a configuration may hold at most 2**31 - 1 rays")
         offs = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
         self.counts = counts
         self.ray_offset_host = offs

@@ -12,7 +12,6 @@
 #include <stdint.h>
 #include <string.h>
 
-#include <mutex>
 
 #include "../../include/optika_gb300.h"
 #include "batch_rays.cuh"
@@ -190,8 +189,10 @@ namespace otx {
 // Tile list of a batch, built on the device from the ray-count prefix sums:
 // one CTA, each thread owning a contiguous run of configurations, a block
 // scan of their tile counts, then every thread writing its tiles.  Writes
-// are bounded by num_tiles; entries the prefix sums leave unwritten carry
-// config -1, which the trace kernel skips.
+// are bounded by num_tiles (the scratch array's capacity); entries past the
+// batch's own tiles carry config -1, which the trace kernel skips.  A work
+// item holds its first ray as int32, so a configuration of more than
+// 2^31 - 1 rays gets no tiles (the host API rejects such counts).
 __global__ void __launch_bounds__(1024) k_make_tiles(const int64_t* __restrict__ offs,
                                                     int num_configs, int tile_size,
                                                     int64_t num_tiles, int32_t* __restrict__ tiles) {
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(1024) k_make_tiles(const int64_t* __restrict__
   int64_t mine = 0;
   for (int c = c0; c < c1; ++c) {
     const int64_t n = offs[c + 1] - offs[c];
-    mine += n > 0 ? (n + tile_size - 1) / tile_size : 0;
+    if (n > 0 && n <= INT32_MAX) mine += (n + tile_size - 1) / tile_size;
   }
   sums[tid] = mine;
   __syncthreads();
@@ -215,6 +216,7 @@ __global__ void __launch_bounds__(1024) k_make_tiles(const int64_t* __restrict__
   int64_t t = sums[tid] - mine;  // exclusive prefix
   for (int c = c0; c < c1; ++c) {
     const int64_t n = offs[c + 1] - offs[c];
+    if (n > INT32_MAX) continue;
     for (int64_t start = 0; start < n && t < num_tiles; start += tile_size, ++t) {
       tiles[2 * t] = c;
       tiles[2 * t + 1] = (int32_t)start;
@@ -227,20 +229,15 @@ __global__ void __launch_bounds__(1024) k_make_tiles(const int64_t* __restrict__
   }
 }
 
-static std::mutex g_noalloc_mutex;
-static int32_t* g_noalloc_ptr[64];
-
-// Device address of the scratch array for the current device, resolved
-// once per device (with that device current) by cudaGetSymbolAddress.
-static int32_t* noalloc_scratch(int dev) {
-  if (dev < 0 || dev >= 64) return nullptr;
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return nullptr;
-    g_noalloc_ptr[dev] = static_cast<int32_t*>(p);
-  }
-  return g_noalloc_ptr[dev];
+// Device address of the scratch array on the current device.  The host
+// name g_noalloc_scratch is only a stand-in for the array; its address in
+// the current context comes from cudaGetSymbolAddress (which allocates
+// nothing), looked up on every call so that a context recreated since the
+// last call (after cudaDeviceReset, say) is never given a stale pointer.
+static int32_t* noalloc_scratch() {
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return nullptr;
+  return static_cast<int32_t*>(p);
 }
 
 }  // namespace otx
@@ -275,7 +272,7 @@ extern "C" otx_status otx_trace_batch_noalloc(const otx_system* base, const otx_
 
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return OTX_ERR_CUDA;
-  int32_t* scratch = noalloc_scratch(dev);
+  int32_t* scratch = noalloc_scratch();
   if (!scratch) return OTX_ERR_CUDA;
   int32_t* counter = scratch;
   int32_t* tiles = scratch + OTX_NOALLOC_HEADER_WORDS;
@@ -285,11 +282,17 @@ extern "C" otx_status otx_trace_batch_noalloc(const otx_system* base, const otx_
   S.inv_width_x = S.width_x > 0.f ? 1.f / S.width_x : 0.f;
   S.inv_width_y = S.width_y > 0.f ? 1.f / S.width_y : 0.f;
   S.inv_width_w = (S.w_hi > S.w_lo) ? (float)S.num_w / (S.w_hi - S.w_lo) : 0.f;
+  // The tile list is built on the device from the ray offsets and padded
+  // to the array's capacity, and the trace takes work items up to that
+  // capacity (padding items are skipped): the caller's num_tiles, which
+  // the host cannot check against device-resident offsets, is used only
+  // for the size check above.
   BatchArgs a;
   memset(&a, 0, sizeof(a));
   a.b = b;
   a.b.tiles = reinterpret_cast<uint64_t>(tiles);
   a.b.counter = reinterpret_cast<uint64_t>(counter);
+  a.b.num_tiles = OTX_NOALLOC_MAX_TILES;
   a.out = *out;
   if (bin) a.img = *image;
 
@@ -298,13 +301,12 @@ extern "C" otx_status otx_trace_batch_noalloc(const otx_system* base, const otx_
   if (cudaMemsetAsync(counter, 0, OTX_NOALLOC_HEADER_WORDS * sizeof(int32_t), st) != cudaSuccess)
     return OTX_ERR_CUDA;
   k_make_tiles<<<1, 1024, 0, st>>>(reinterpret_cast<const int64_t*>(b.ray_offset), b.num_configs,
-                                   b.tile_size, b.num_tiles, tiles);
+                                   b.tile_size, (int64_t)OTX_NOALLOC_MAX_TILES, tiles);
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (sms <= 0) sms = 132;
   const int per_sm = 2048 / block;
-  int64_t grid = (int64_t)sms * (per_sm < 8 ? per_sm : 8);
-  if (grid > b.num_tiles) grid = b.num_tiles;
+  const int64_t grid = (int64_t)sms * (per_sm < 8 ? per_sm : 8);
   const bool fixed =
       !(launch && launch->generic_only) && shape_matches<BObject, BSphere, BGrating, BSensor>(sys);
   if (fixed)

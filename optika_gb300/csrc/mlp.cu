@@ -335,13 +335,10 @@ static otx_status launch_gemm(const CUtensorMap& ta, const CUtensorMap& tb, cons
                               int splits, cudaStream_t st) {
   const size_t smem = 1024 + GEMM_STAGES * (128 * GEMM_BK * 2 + NT * GEMM_BK * 2) +
                       (2 * GEMM_STAGES + 2) * 8;
-  static bool configured = false;
-  if (!configured) {
-    if (cudaFuncSetAttribute(k_gemm<NT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
-      return OTX_ERR_CUDA;
-    configured = true;
-  }
+  // per-context function attribute: set on every launch (cheap)
+  if (cudaFuncSetAttribute(k_gemm<NT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    return OTX_ERR_CUDA;
   const dim3 grid((g.m + 127) / 128, splits);
   k_gemm<NT, EPI><<<grid, 128, smem, st>>>(ta, tb, g);
   return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;

@@ -485,6 +485,9 @@ otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* ba
   if (b.num_configs < 1 || !b.ray_offset || sg->num_configs != b.num_configs ||
       !sg->config_inputs || !sg->baseline || !(sg->out_scale > 0.f))
     return OTX_ERR_INVALID;
+  // the fallback kernel's grid holds one configuration per y index (at most
+  // 65535): reject larger batches before any GPU work
+  if (b.num_configs > 65535) return OTX_ERR_SIZE;
   if (const otx_status vs = validate_system(base)) return vs;
   if (base->input_mode != OTX_INPUT_GRID_INFINITY) return OTX_ERR_INVALID;
   if (!(base->flags & OTX_SYS_FLAG_FINAL_IDENTITY)) return OTX_ERR_UNSUPPORTED;
@@ -561,13 +564,12 @@ otx_status otx_surrogate_image_fused(const otx_system* base, const otx_batch* ba
   a.err = err;
   a.predict = reinterpret_cast<float4*>(predict);
 
-  static bool configured = false;
-  if (!configured) {
-    if (cudaFuncSetAttribute(k_surrogate_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)F_SMEM) != cudaSuccess)
-      return OTX_ERR_CUDA;
-    configured = true;
-  }
+  // the shared-memory limit is an attribute of the function in the current
+  // device's context: set on every call (cheap), so every device a process
+  // drives gets it
+  if (cudaFuncSetAttribute(k_surrogate_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)F_SMEM) != cudaSuccess)
+    return OTX_ERR_CUDA;
   const int64_t grid = a.num_pairs < sms ? a.num_pairs : sms;
   k_surrogate_fused<<<(unsigned)grid, F_THREADS, F_SMEM, st>>>(maps, a);
   if (cudaGetLastError() != cudaSuccess) return OTX_ERR_CUDA;

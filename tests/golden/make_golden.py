@@ -4,13 +4,13 @@ The reference pins ``multilayer_efficiency`` against IMD output files
 (optika/materials/_tests/test_multilayers.py:178-287, data in
 optika/materials/_tests/_data/*.txt, normal incidence, rtol 1e-4), computed
 with the optical constants of optika/chemicals/nk/*.nk.  This script reads
-both from a reference checkout (default /root/reference), keeps every
+both from a checkout of the reference given on the command line, keeps every
 ``STEP``-th wavelength, and stores per case the IMD efficiency and, for each
 chemical of the stack, n and k linearly interpolated at those wavelengths
 (the reference's ``na.interp`` of the table, optika/chemicals/_chemicals.py:
 138-142).  Run it where the reference is available:
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py /path/to/optika
 """
 
 from __future__ import annotations
@@ -71,4 +71,6 @@ def main(ref: pathlib.Path) -> None:
 
 
 if __name__ == "__main__":
-    main(pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path to the optika source tree>")
+    main(pathlib.Path(sys.argv[1]))

@@ -226,6 +226,10 @@ def test_fused_surrogate_validation(built_library):
     assert call(net_=net2) == L.ERR_INVALID
     s2 = _system(4)
     assert call(sys_=s2) == L.ERR_UNSUPPORTED  # outputs must be in the sensor frame
+    # more configurations than the fallback grid's y dimension holds
+    b.num_configs = sg.num_configs = 65536
+    assert call() == L.ERR_SIZE
+    b.num_configs = sg.num_configs = 2
 
 
 def test_rulings_cells_expose_reduce_validation(built_library):

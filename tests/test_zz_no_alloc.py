@@ -74,6 +74,24 @@ def test_noalloc_batch_matches_regular_entry(cuda):
             assert torch.allclose(bufs[k][m], ref[k][m], atol=1e-6, rtol=0), k
         assert torch.equal(images, ref_img)
 
+    # the library counts the tiles itself: a caller's count that is too
+    # large or too small (but within the array) traces the same rays
+    for num_tiles in (b.num_tiles + 100, 1):
+        b2 = L.Batch()
+        ctypes.memmove(ctypes.byref(b2), ctypes.byref(b), ctypes.sizeof(L.Batch))
+        b2.num_tiles = num_tiles
+        bufs, out = _outputs(bt, torch)
+        images = torch.zeros_like(bt.images)
+        img = L.Image()
+        img.counts = images.data_ptr()
+        st = lib.otx_trace_batch_noalloc(ctypes.byref(bt.lowering.sys), ctypes.byref(b2),
+                                         ctypes.byref(out), ctypes.byref(img),
+                                         ctypes.byref(bt.launch), stream_handle())
+        assert st == L.OK, lib.otx_status_string(st)
+        torch.cuda.synchronize()
+        assert torch.equal(bufs["unvignetted"], ref["unvignetted"])
+        assert torch.equal(images, ref_img)
+
     # sizes beyond the scratch array are rejected, before any GPU work
     big = L.Batch()
     ctypes.memmove(ctypes.byref(big), ctypes.byref(b), ctypes.sizeof(L.Batch))
