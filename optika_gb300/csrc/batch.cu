@@ -43,6 +43,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const __grid_constant__ otx
   const int32_t* tiles = reinterpret_cast<const int32_t*>(b.tiles);
   unsigned int* counter = reinterpret_cast<unsigned int*>(b.counter);
   const bool bin = image_any(a.img);
+  int bin_skip = 0;
   int cur = -1;
   for (;;) {
     __syncthreads();  // previous item done: s_item and surf may be rewritten
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const __grid_constant__ otx
             if (img.counts) img.counts += off * 4;
             if (img.flux) img.flux += off * 4;
             if (img.cos_moment) img.cos_moment += off * 4;
-            bin_ray(sys.sensor, img, r[k]);
+            bin_ray_warp(sys.sensor, img, r[k], bin_skip);
           }
           store_ray<true>(a.out, base + i, sys.final_to_output, r[k]);
         }
@@ -128,7 +129,8 @@ extern "C" otx_status otx_trace_batch(const otx_system* base, const otx_batch* b
   const bool bin = image && (image->counts || image->flux);
   if (bin && (base->sensor.num_x < 1 || base->sensor.num_y < 1 || base->sensor.num_w < 1 ||
               !(base->sensor.width_x > 0.f) || !(base->sensor.width_y > 0.f) ||
-              b.image_stride < base->sensor.num_w * base->sensor.num_x * base->sensor.num_y))
+              (int64_t)b.image_stride < (int64_t)base->sensor.num_w * base->sensor.num_x *
+                                            base->sensor.num_y))
     return OTX_ERR_INVALID;
   int rpt = (launch && launch->rays_per_thread > 0) ? launch->rays_per_thread : 1;
   if (rpt != 1 && rpt != 2) return OTX_ERR_INVALID;
@@ -263,7 +265,8 @@ extern "C" otx_status otx_trace_batch_noalloc(const otx_system* base, const otx_
   const bool bin = image && (image->counts || image->flux);
   if (bin && (base->sensor.num_x < 1 || base->sensor.num_y < 1 || base->sensor.num_w < 1 ||
               !(base->sensor.width_x > 0.f) || !(base->sensor.width_y > 0.f) ||
-              b.image_stride < base->sensor.num_w * base->sensor.num_x * base->sensor.num_y))
+              (int64_t)b.image_stride < (int64_t)base->sensor.num_w * base->sensor.num_x *
+                                            base->sensor.num_y))
     return OTX_ERR_INVALID;
   int rpt = (launch && launch->rays_per_thread > 0) ? launch->rays_per_thread : 1;
   if (rpt != 1 && rpt != 2) return OTX_ERR_INVALID;

@@ -83,6 +83,8 @@ static otx_status validate_image(const otx_system* sys, const otx_image* img) {
   if (!img || !image_any(*img)) return OTX_OK;
   const otx_sensor& S = sys->sensor;
   if (S.num_x < 1 || S.num_y < 1 || S.num_w < 1) return OTX_ERR_INVALID;
+  // pixel indices are int32 in the binning
+  if ((int64_t)S.num_w * S.num_x * S.num_y > INT32_MAX) return OTX_ERR_SIZE;
   if (!(S.width_x > 0.f) || !(S.width_y > 0.f)) return OTX_ERR_INVALID;
   return OTX_OK;
 }

@@ -135,19 +135,22 @@ __device__ __forceinline__ void store_ray(const otx_rays& o, int64_t i,
 
 // Histogram bin of a ray in the sensor frame, numpy.histogramdd edges:
 // [e_j, e_j+1) with the last edge inclusive; outside and NaN are dropped
-// (optika/sensors/_sensors.py:141-155).
+// (optika/sensors/_sensors.py:141-155).  Every operation is explicitly
+// rounded (no contraction), so a float32 restatement of this formula
+// reproduces each ray's bin exactly: upper edge lo + num w as one fused
+// multiply-add, bin floor((p - lo) * (1 / w)).
 __device__ __forceinline__ int64_t sensor_bin(const otx_sensor& S, const Ray& r) {
-  const float hx = S.lo_x + S.num_x * S.width_x;
-  const float hy = S.lo_y + S.num_y * S.width_y;
+  const float hx = __fmaf_rn((float)S.num_x, S.width_x, S.lo_x);
+  const float hy = __fmaf_rn((float)S.num_y, S.width_y, S.lo_y);
   if (!(r.px >= S.lo_x && r.px <= hx && r.py >= S.lo_y && r.py <= hy)) return -1;
-  int ix = (int)floorf((r.px - S.lo_x) * S.inv_width_x);
-  int iy = (int)floorf((r.py - S.lo_y) * S.inv_width_y);
+  int ix = (int)floorf(__fmul_rn(__fsub_rn(r.px, S.lo_x), S.inv_width_x));
+  int iy = (int)floorf(__fmul_rn(__fsub_rn(r.py, S.lo_y), S.inv_width_y));
   ix = min(max(ix, 0), S.num_x - 1);
   iy = min(max(iy, 0), S.num_y - 1);
   int iw = 0;
   if (S.w_hi > S.w_lo) {
     if (!(r.wl >= S.w_lo && r.wl <= S.w_hi)) return -1;
-    iw = (int)floorf((r.wl - S.w_lo) * S.inv_width_w);
+    iw = (int)floorf(__fmul_rn(__fsub_rn(r.wl, S.w_lo), S.inv_width_w));
     iw = min(max(iw, 0), S.num_w - 1);
   }
   return ((int64_t)iw * S.num_x + ix) * S.num_y + iy;
@@ -162,6 +165,66 @@ __device__ __forceinline__ void bin_ray(const otx_sensor& S, const otx_image& im
   if (img.flux) atomicAdd(reinterpret_cast<float*>(img.flux) + b, r.inten);
   // cosine of incidence on the flat sensor (normal -z in its frame): dz
   if (img.cos_moment) atomicAdd(reinterpret_cast<float*>(img.cos_moment) + b, r.inten * r.dz);
+}
+
+// Sensor binning of the trace kernels with warp aggregation.  A warp first
+// counts its lanes whose pixel equals their left neighbour's (one shuffle and
+// one ballot).  Rays spread over the sensor (the precision workload's random
+// fields) rarely share a pixel: those warps add with plain atomics, and skip
+// the test for their next 7 rays (`skip`, a per-thread counter the kernel
+// keeps across its loop; a warp's lanes update it alike), since whether a
+// warp's rays repeat pixels follows from the ray order and persists.  When
+// several lanes repeat a pixel (a warp of rays from one field point of a
+// telescope lands in a handful of pixels), the active lanes of each pixel
+// form one group (__match_any_sync on the bin index), sum their
+// intensities (and cosine moments) by shared-memory atomics into the group
+// leader's slot, and the leader adds the group's count and sums to the
+// images with one global atomic each, so the atomics on those contended
+// addresses fall by up to 32x.  Counts are exact integers however the lanes
+// group; the float sums are order-dependent within FP32 rounding, as any
+// atomic sum is.  Blocks of up to OTX_BIN_MAX_THREADS threads (the trace
+// kernels' limit; larger blocks bin with plain atomics); image indices fit
+// int32 (the host checks the image size).
+#define OTX_BIN_MAX_THREADS 256
+__device__ __forceinline__ void bin_ray_warp(const otx_sensor& S, const otx_image& img,
+                                             const Ray& r, int& skip) {
+  __shared__ float s_flux[OTX_BIN_MAX_THREADS], s_mom[OTX_BIN_MAX_THREADS];
+  if (skip > 0 || blockDim.x > OTX_BIN_MAX_THREADS) {
+    --skip;
+    bin_ray(S, img, r);
+    return;
+  }
+  const unsigned mask = __activemask();
+  const int b = r.ok ? (int)sensor_bin(S, r) : -1;
+  const int lane = threadIdx.x & 31;
+  const int prev = __shfl_up_sync(mask, b, 1);
+  const bool repeat = b >= 0 && lane > 0 && ((mask >> (lane - 1)) & 1u) && prev == b;
+  if (__popc(__ballot_sync(mask, repeat)) < 4) {
+    skip = 7;
+    bin_ray(S, img, r);
+    return;
+  }
+  const unsigned peers = __match_any_sync(mask, b);
+  const int leader = __ffs(peers) - 1;
+  const int slot = (threadIdx.x & ~31) + leader;
+  const bool lead = lane == leader;
+  const bool mom = img.cos_moment != 0;
+  if (lead) {
+    s_flux[threadIdx.x] = 0.f;
+    if (mom) s_mom[threadIdx.x] = 0.f;
+  }
+  __syncwarp(mask);
+  if (b >= 0) {
+    atomicAdd(&s_flux[slot], r.inten);
+    // cosine of incidence on the flat sensor (normal -z in its frame): dz
+    if (mom) atomicAdd(&s_mom[slot], r.inten * r.dz);
+  }
+  __syncwarp(mask);
+  if (lead && b >= 0) {
+    if (img.counts) atomicAdd(reinterpret_cast<unsigned int*>(img.counts) + b, (unsigned)__popc(peers));
+    if (img.flux) atomicAdd(reinterpret_cast<float*>(img.flux) + b, s_flux[threadIdx.x]);
+    if (mom) atomicAdd(reinterpret_cast<float*>(img.cos_moment) + b, s_mom[threadIdx.x]);
+  }
 }
 
 // Minimum resident CTAs per SM requested from the register allocator
@@ -179,6 +242,7 @@ __global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
   const int ns = sys.num_surfaces;
   const bool bin = image_any(a.img);
   const bool final_identity = (sys.flags & OTX_SYS_FLAG_FINAL_IDENTITY) != 0;
+  int bin_skip = 0;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x * RPT + threadIdx.x; base < n;
        base += step) {
     Ray r[RPT];
@@ -202,7 +266,7 @@ __global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
     for (int k = 0; k < RPT; ++k) {
       const int64_t i = base + (int64_t)k * blockDim.x;
       if (i < n) {
-        if (bin) bin_ray(sys.sensor, a.img, r[k]);
+        if (bin) bin_ray_warp(sys.sensor, a.img, r[k], bin_skip);
         if (!ACC) {
           if (final_identity)
             store_ray<true>(a.out, i, sys.final_to_output, r[k]);
@@ -242,8 +306,11 @@ __device__ __forceinline__ bool first_is_noop(const otx_system& sys) {
   }
 }
 
+// The shape-specialised kernels keep 4 CTAs of 256 threads resident per SM
+// (at most 64 registers per thread): they are bound by instruction issue,
+// and 3 CTAs per SM lose ~9 % of it.
 template <int MODE, class K0, class... Ks>
-__global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
+__global__ void __launch_bounds__(256, 4)
     k_trace_fixed(const __grid_constant__ otx_system sys,
                   const __grid_constant__ TraceArgs a) {
   const int64_t n = a.count;
@@ -251,12 +318,13 @@ __global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
   const bool bin = image_any(a.img);
   const bool final_identity = (sys.flags & OTX_SYS_FLAG_FINAL_IDENTITY) != 0;
   const bool skip0 = first_is_noop<MODE, K0>(sys);
+  int bin_skip = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
     Ray r;
     load_ray<MODE>(a, i, r);
     if (!skip0) propagate_surface<K0, false>(sys, sys.surfaces[0], r);
     if constexpr (sizeof...(Ks) > 0) propagate_fixed<1, Ks...>(sys, r);
-    if (bin) bin_ray(sys.sensor, a.img, r);
+    if (bin) bin_ray_warp(sys.sensor, a.img, r, bin_skip);
     if (final_identity)
       store_ray<true>(a.out, i, sys.final_to_output, r);
     else
