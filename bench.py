@@ -222,6 +222,27 @@ def peaks() -> tuple[dict, str]:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def fp32_roofline(workload: str, units: int, ms: float, pk: dict) -> dict | None:
+    """The FP32 roofline of a workload from its frozen algorithmic counts
+    (profiles/algorithmic_counts.json, made by oracle/freeze_counts.py):
+    algorithmic flops per unit x units over the kernel's time, against the
+    FP32 pipe's nominal peak at the measured maximum SM clock (152 SMs x 128
+    lanes x 2 flops per FMA)."""
+    p = ROOT / "profiles" / "algorithmic_counts.json"
+    if not p.exists():
+        return None
+    c = json.loads(p.read_text()).get(workload)
+    if not c:
+        return None
+    peak = 152 * 128 * 2 * float(pk.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    ach = c["flops"] * units / (ms * 1e-3) / 1e12
+    return {"achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+            "algorithmic_flops_per_unit": c["flops"], "algorithmic_div_per_unit": c["div"],
+            "algorithmic_special_per_unit": c["special"], "per": c["unit"],
+            "counted_by": "oracle/flops.py via oracle/freeze_counts.py",
+            "peak_kind": "nominal at the measured maximum SM clock"}
+
+
 def run_reference(args, rank: int, world: int) -> None:
     if rank != 0:
         return
@@ -466,6 +487,7 @@ def run_batched(args, rank: int, world: int, emit: bool = True) -> dict:
                          "frac": ach / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
                          "bytes_per_ray": bpr, "kernel": "k_trace_batch (spectrograph shape)",
                          "kernel_ms": ms,
+                         "fp32": fp32_roofline("batched-spectrograph", total, ms, pk),
                          "note": "compute-bound (FP32 issue): the byte roofline is shown for "
                                  "completeness"},
             "cpu_baseline": cpu, "gpu_launches": 3, "clocks": clk,
@@ -578,6 +600,7 @@ def run_multilayer(args, rank: int, world: int, emit: bool = True) -> dict:
                          "frac": ach / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
                          "bytes_per_sample": bps, "kernel": "k_multilayer_periodic",
                          "kernel_ms": ms,
+                         "fp32": fp32_roofline("multilayer-periodic", n, ms, pk),
                          "note": "compute-bound (FP32 issue): the byte roofline is shown for "
                                  "completeness"},
             "cpu_baseline": cpu, "gpu_launches": args.steps, "clocks": clk,

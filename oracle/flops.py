@@ -262,3 +262,20 @@ def count_rayfunction(system, grid: dict) -> dict:
     out = COUNTS.per(n)
     COUNTS.clear()
     return out
+
+
+def count_multilayer(layers, substrate, wavelength, cos_incidence, n=1.0) -> dict:
+    """Per-sample operation counts of ``oracle.trace.multilayer_efficiency``
+    (R and T for s and p; the reference's periodic block as its first
+    period times the period matrix to the power num_periods - 1, by binary
+    powering, optika/materials/_layers.py:611-645)."""
+    from oracle import trace as O
+
+    m = len(np.atleast_1d(wavelength))
+    COUNTS.clear()
+    O.multilayer_efficiency(np.asarray(wavelength, dtype=np.float64).view(Counted),
+                            np.asarray(cos_incidence, dtype=np.float64).view(Counted), n,
+                            layers, substrate)
+    out = COUNTS.per(m)
+    COUNTS.clear()
+    return out

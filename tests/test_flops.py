@@ -69,3 +69,13 @@ def test_count_does_not_change_the_oracle():
     again = O.rayfunction(s, **g)
     for k in ("px", "py", "opl", "intensity"):
         assert np.array_equal(plain[k], again[k], equal_nan=True)
+
+
+def test_frozen_workload_counts_match_the_counter():
+    from oracle import freeze_counts
+
+    frozen = json.loads((ROOT / "profiles" / "algorithmic_counts.json").read_text())
+    for name, fresh in (("batched-spectrograph", freeze_counts.batched_counts(2, 1000)),
+                        ("multilayer-periodic", freeze_counts.multilayer_counts(2, 1000))):
+        for k in ("flops", "div", "special"):
+            assert fresh[k] == pytest.approx(frozen[name][k], rel=1e-2), (name, k)
