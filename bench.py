@@ -745,10 +745,12 @@ def _cpu_stops_worker(args):
 
 def run_stops(args, rank: int, world: int) -> None:
     """The stop solver: field and pupil extents of the grazing-incidence
-    spectrograph at 16 wavelengths (21 x 21 boundary ray pairs each, Newton
-    to convergence, the backward trace), all wavelengths in one batched
-    solve.  Host-driven and latency-bound: a step is the public call
-    ``extents_many`` with the cache cleared; replicas under torchrun."""
+    spectrograph at --stop-wavelengths wavelengths (default 64; 21 x 21
+    boundary ray pairs each), all wavelengths in one batched solve: the
+    Newton iterations in one kernel launch (otx_stop_newton), then the
+    backward trace and the extents.  A step is the public call
+    ``extents_many`` with the extents cleared (the lowered descriptors stay
+    cached on the system, as in repeated use); replicas under torchrun."""
     import torch
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
@@ -758,7 +760,7 @@ def run_stops(args, rank: int, world: int) -> None:
     from optika_gb300 import stops as stops_mod
 
     system = configs.stop_grazing()
-    wls = np.linspace(500.0, 600.0, 16)
+    wls = np.linspace(500.0, 600.0, args.stop_wavelengths)
     launches = [0]
     trace = stops_mod._trace
 
@@ -808,8 +810,8 @@ def run_stops(args, rank: int, world: int) -> None:
                        "boundary_pairs": 441, "system": "grazing spectrograph"},
             "roofline": {"bound": "hbm", "achieved": None, "peak": pk["hbm_gbs"], "unit": "GB/s",
                          "frac": None, "traffic": None, "peak_kind": pk_kind,
-                         "note": "latency-bound: a few thousand rays per launch, one host "
-                                 "convergence check per Newton iteration"},
+                         "note": "latency-bound: one Newton launch of a few thousand rays, the "
+                                 "backward trace and the host setup around them"},
             "e2e": {"value": value, "unit": "solves/s", "ms_per_step": ms,
                     "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 16 * len(wls) * 8},
             "cpu_baseline": cpu, "gpu_launches": traces, "clocks": clk,
@@ -828,6 +830,8 @@ def main() -> None:
     ap.add_argument("--ref-rays", type=int, default=2_000_000,
                     help="rays per step of the reference (CPU) arm")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--stop-wavelengths", type=int, default=64,
+                    help="wavelengths per stop solve (--workload stops)")
     ap.add_argument("--no-workloads", action="store_true",
                     help="time the precision form only (no batched, multilayer, surrogate)")
     ap.add_argument("--workload", default="precision",

@@ -554,6 +554,37 @@ int64_t otx_surrogate_image_fused_workspace(const otx_batch* batch, const otx_ml
 otx_status otx_collect(const otx_sensor* sensor, const otx_rays* rays,
                        const otx_image* image, void* stream);
 
+/* Newton solve of the stop rays, one thread per ray (a pair of stop
+ * boundary points at one wavelength).
+ * Replaces the Newton loop of optika/systems/_sequential.py:396-693
+ * (_calc_rayfunction_stops_only, its _ray_error at :363-394): the free
+ * component (x, y) of each ray at the first stop -- its direction, z then
+ * sqrt(1 - x^2 - y^2), or with `free_position` its position, z the sag of
+ * first_sag->surfaces[0] -- is moved until the ray, traced through `sub`
+ * (the surfaces after the first stop, input in the system frame, output
+ * in sub's final_to_output frame) and mapped by `to_last` (3 x 4 affine,
+ * float64, row-major) lands on (target_x, target_y): the point's or, with
+ * `target_direction`, the direction's first two components.  Each
+ * iteration takes a forward-difference Jacobian with `step`; a ray whose
+ * residual falls below `tolerance` takes `polish_steps` more steps.
+ * position and direction are device float64 [3][count] arrays (in: the
+ * starting rays; out: the solved ones); wavelength, target_x, target_y
+ * device float64 [count]; status device int32 [count]: the iteration at
+ * which the ray finished, -1 if it did not within max_iterations. */
+typedef struct otx_stop_solve {
+  int64_t count;
+  int32_t free_position;    /* 1: the ray's position on the first stop is free */
+  int32_t target_direction; /* 1: the target is the direction at the last stop */
+  int32_t max_iterations;
+  int32_t polish_steps;
+  double step;
+  double tolerance;
+  double to_last[12];
+  uint64_t position, direction, wavelength, target_x, target_y, status;
+} otx_stop_solve;
+otx_status otx_stop_newton(const otx_system* sub, const otx_system* first_sag,
+                           const otx_stop_solve* solve, void* stream);
+
 /* Evaluate the sag of sys->surfaces[0] at `in` positions.
  * mode 0: sag z(x, y) into out->pz   (optika/sags/_abc.py:48-62 __call__)
  * mode 1: unit normal into out->d*   (optika/sags/_abc.py:64-75 normal)

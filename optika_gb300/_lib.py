@@ -218,6 +218,25 @@ class Image(ctypes.Structure):
     _fields_ = [("counts", u64), ("flux", u64), ("cos_moment", u64)]
 
 
+class StopSolve(ctypes.Structure):
+    _fields_ = [
+        ("count", i64),
+        ("free_position", i32),
+        ("target_direction", i32),
+        ("max_iterations", i32),
+        ("polish_steps", i32),
+        ("step", ctypes.c_double),
+        ("tolerance", ctypes.c_double),
+        ("to_last", ctypes.c_double * 12),
+        ("position", u64),
+        ("direction", u64),
+        ("wavelength", u64),
+        ("target_x", u64),
+        ("target_y", u64),
+        ("status", u64),
+    ]
+
+
 class Batch(ctypes.Structure):
     _fields_ = [
         ("num_configs", i32),
@@ -318,6 +337,7 @@ LAYOUT = {
     12: Surrogate,
     13: Mlp,
     14: Cells,
+    15: StopSolve,
 }
 
 LIB_PATH = pathlib.Path(__file__).resolve().parent / "_lib" / "liboptika_gb300.so"
@@ -370,6 +390,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_trace_batch.restype = i32
     lib.otx_trace_batch_noalloc.argtypes = [P(System), P(Batch), P(Rays), P(Image), P(Launch), v]
     lib.otx_trace_batch_noalloc.restype = i32
+    lib.otx_stop_newton.argtypes = [P(System), P(System), P(StopSolve), v]
+    lib.otx_stop_newton.restype = i32
     lib.otx_gemm_bf16.argtypes = [v, i32, v, i32, i32, i32, i32, v, i32, v, i32, v, v, i32, v, v]
     lib.otx_gemm_bf16.restype = i32
     lib.otx_silu_backward.argtypes = [v, v, v, i64, v]

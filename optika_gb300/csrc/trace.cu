@@ -473,6 +473,7 @@ int64_t otx_sizeof(int32_t which) {
     case 12: return sizeof(otx_surrogate);
     case 13: return sizeof(otx_mlp);
     case 14: return sizeof(otx_cells);
+    case 15: return sizeof(otx_stop_solve);
     default: return -1;
   }
 }

@@ -10,15 +10,18 @@ For every pair of a point on the first stop's boundary and a point on the
 last stop's (21 x 21 pairs), Newton's method finds the free component of
 the ray at the first stop (its direction, or its position when the first
 stop's aperture is angular) that lands the ray on the target point of the
-last stop.  Each Newton iteration evaluates the rays and their two
-finite-difference perturbations in ONE launch of the trace kernel
-(``otx_trace_rays`` over the surfaces between the stops); the 2 x 2 updates
-run on the same device tensors.  The solved rays are then traced back to
-the object surface (the reversed surface list, as the reference does).
+last stop.  The whole Newton solve runs in one kernel launch
+(``otx_stop_newton``): one thread per ray traces it and its two
+finite-difference perturbations through the surfaces between the stops in
+every iteration and applies the 2 x 2 update, with no host round trip.
+The solved rays are then traced back to the object surface (the reversed
+surface list, as the reference does).
 
 The trace is FP32, so the convergence test uses the larger of the
 reference's 1e-9 (times the target aperture's size) and a floor of 4e-7 of
-it, and two further Newton steps polish each root to the trace's noise;
+it, and two further Newton steps polish each ray's root to the trace's
+noise (the reference stops when every ray has converged; here each ray
+stops on its own);
 the extents agree with the float64 restatement to ~1e-6 relative (see the
 tests).
 """
@@ -78,6 +81,12 @@ def _sag(sag, x: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
     return sag(Cartesian2dVectorArray(x.float(), y.float())).to(torch.float64)
 
 
+def _api_sag_system(sag):
+    from ._api import _sag_system
+
+    return _sag_system(sag)
+
+
 def _lower(surfaces: Sequence):
     """The descriptor of ``surfaces`` for repeated traces within one solve."""
     from . import _lib as L
@@ -85,6 +94,16 @@ def _lower(surfaces: Sequence):
 
     return lower_surfaces(list(surfaces), pre=np.eye(4), final=None, input_mode=L.INPUT_RAYS,
                           device=device())
+
+
+def _cached(system, key, make):
+    """A descriptor lowered once per system and key: the stop solve of a
+    system repeats for every batch of wavelengths, and the extents it gives
+    are cached on the system the same way."""
+    cache = system.__dict__.setdefault("_stop_lowerings", {})
+    if key not in cache:
+        cache[key] = make()
+    return cache[key]
 
 
 def _trace(surfaces: Sequence, p: torch.Tensor, d: torch.Tensor, wavelength, lowering=None):
@@ -117,6 +136,48 @@ def _trace(surfaces: Sequence, p: torch.Tensor, d: torch.Tensor, wavelength, low
         _api.stream_handle()), "otx_trace_rays")
     o = out.to(torch.float64)
     return o[:3], o[3:]
+
+
+def _newton(lowering, first, pos_f, dir_f, wl_f, tx, ty, Tl, *, free_position: bool,
+            target_direction: bool, step: float, tol: float, names: tuple) -> None:
+    """The Newton iterations of every ray on the device (otx_stop_newton):
+    ``pos_f`` / ``dir_f`` ([3, n] float64, system frame) are updated in
+    place with the solved rays.  One thread per ray: each iteration traces
+    the ray and its two finite-difference perturbations and applies the
+    2 x 2 update; a ray whose residual drops below ``tol`` takes two more
+    steps.  The host reads only the per-ray status at the end."""
+    import ctypes
+
+    from . import _api
+    from . import _lib as L
+
+    n = pos_f.shape[1]
+    dev = pos_f.device
+    f64 = torch.float64
+    pos = pos_f.to(f64).contiguous()
+    dirn = dir_f.to(f64).contiguous()
+    wl = wl_f.to(f64).contiguous()
+    txc, tyc = tx.to(f64).contiguous(), ty.to(f64).contiguous()
+    status = torch.empty(n, dtype=torch.int32, device=dev)
+    sol = L.StopSolve()
+    sol.count = n
+    sol.free_position = int(free_position)
+    sol.target_direction = int(target_direction)
+    sol.max_iterations = MAX_ITER
+    sol.polish_steps = 2
+    sol.step = float(step)
+    sol.tolerance = float(tol)
+    for k, v in enumerate(Tl[:3, :4].reshape(-1).cpu().tolist()):
+        sol.to_last[k] = v
+    sol.position, sol.direction, sol.wavelength = (_api.ptr(t) for t in (pos, dirn, wl))
+    sol.target_x, sol.target_y, sol.status = (_api.ptr(t) for t in (txc, tyc, status))
+    L.check(L.load().otx_stop_newton(ctypes.byref(lowering.sys), ctypes.byref(first),
+                                     ctypes.byref(sol), _api.stream_handle()), "otx_stop_newton")
+    if bool((status < 0).any()):
+        raise ValueError(f"could not solve for the rays connecting the stop surfaces "
+                         f"{names[0]!r} and {names[1]!r}")
+    pos_f.copy_(pos)
+    dir_f.copy_(dirn)
 
 
 def stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
@@ -165,11 +226,6 @@ def stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
             pos = torch.zeros((3,) + shape, dtype=f64, device=dev)
             variable = "position"
 
-        def zf(x, y):
-            if variable == "direction":
-                return torch.sqrt(1 - (x * x + y * y))
-            return _sag(s_first.sag, x, y)
-
         # seed: aim at the first surface with power, or at the target itself
         anchor = anchor_surface(sub)
         if anchor is s_last and not s_last.aperture.dimensionless:
@@ -205,57 +261,17 @@ def stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
         dx = 1e-4 if variable == "direction" else 1e-4 * unit
         Tl = _inverse(_matrix(s_last.transformation))
         # every wavelength repeats the grid (wavelength-major)
-        n = nw * shape[0] * shape[1]
         pos_f = pos.reshape(3, -1).repeat(1, nw)
         dir_f = dirn.reshape(3, -1).repeat(1, nw)
         tx = tx.repeat(nw)
         ty = ty.repeat(nw)
         wl_f = torch.as_tensor(wls, dtype=f64, device=dev).repeat_interleave(shape[0] * shape[1])
 
-        lw_sub = _lower(sub[1:])
-
-        def residuals(xs, ys):
-            """Residuals of len(xs) / n stacked evaluations in one launch."""
-            k = xs.shape[0] // n
-            p = pos_f.repeat(1, k)
-            d = dir_f.repeat(1, k)
-            v = d if variable == "direction" else p
-            v[0], v[1], v[2] = xs, ys, zf(xs, ys)
-            po, do = _trace(sub[1:], p, d, wl_f.repeat(k), lw_sub)
-            if target == "direction":
-                c = _apply(Tl, do, point=False)
-            else:
-                c = _apply(Tl, po)
-            return c[0] - tx.repeat(k), c[1] - ty.repeat(k)
-
-        v0 = dir_f if variable == "direction" else pos_f
-        x, y = v0[0].clone(), v0[1].clone()
-        polish = -1
-        for _ in range(MAX_ITER):
-            xs = torch.cat([x, x + dx, x])
-            ys = torch.cat([y, y, y + dx])
-            rx, ry = residuals(xs, ys)
-            fx, fy = rx[:n], ry[:n]
-            err = torch.maximum(fx.abs(), fy.abs())
-            if polish < 0 and bool((err < tol).all()):
-                polish = 2
-            if polish == 0:
-                break
-            j11, j21 = (rx[n:2 * n] - fx) / dx, (ry[n:2 * n] - fy) / dx
-            j12, j22 = (rx[2 * n:] - fx) / dx, (ry[2 * n:] - fy) / dx
-            det = j11 * j22 - j12 * j21
-            ok = torch.isfinite(det) & (det != 0)
-            sx = torch.where(ok, (j22 * fx - j12 * fy) / det, 0.0)
-            sy = torch.where(ok, (-j21 * fx + j11 * fy) / det, 0.0)
-            x, y = x - sx, y - sy
-            if polish > 0:
-                polish -= 1
-        else:
-            raise ValueError(
-                f"could not solve for the rays connecting the stop surfaces "
-                f"{s_first.name!r} and {s_last.name!r}")
-        v = dir_f if variable == "direction" else pos_f
-        v[0], v[1], v[2] = x, y, zf(x, y)
+        lw_sub = _cached(system, ("sub", first_i, last_i), lambda: _lower(sub[1:]))
+        first = _cached(system, ("sag", first_i), lambda: _api_sag_system(s_first.sag))
+        _newton(lw_sub, first, pos_f, dir_f, wl_f, tx, ty, Tl,
+                free_position=variable == "position", target_direction=target == "direction",
+                step=dx, tol=tol, names=(s_first.name, s_last.name))
         full = (3,) + ((nw,) if not scalar else ()) + shape
         out = dict(position=pos_f.reshape(full), direction=dir_f.reshape(full),
                    wavelength=wl_f.reshape(full[1:]))
@@ -276,7 +292,9 @@ def rayfunction_stops(system, wavelength, samples_pupil: int = SAMPLES_STOP,
     sub = surfaces[min(ip, jf)::-1]
     p, d = st["position"], st["direction"]
     shape = p.shape[1:]
-    po, do = _trace(sub, p.reshape(3, -1), d.reshape(3, -1), st["wavelength"].reshape(-1))
+    lw_back = _cached(system, ("back", min(ip, jf)), lambda: _lower(sub))
+    po, do = _trace(sub, p.reshape(3, -1), d.reshape(3, -1), st["wavelength"].reshape(-1),
+                    lw_back)
     obj = sub[-1]
     Mi = _inverse(_matrix(obj.transformation))
     pl = _apply(Mi, po)
