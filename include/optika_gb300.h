@@ -92,6 +92,8 @@ typedef int32_t otx_status;
  * offsets between surfaces are added, and directions rotated, without
  * FP32 rounding. */
 #define OTX_AFFINE_ROT_IDENTITY 1 /* m is exactly the identity           */
+#define OTX_AFFINE_ROT_Y 2        /* m is a rotation about y: its middle   */
+                                  /* row and column are exactly (0, 1, 0) */
 typedef struct otx_affine {
   float m[9];    /* row-major 3x3 rotation, high parts */
   float m_lo[9]; /* low parts                          */

@@ -48,6 +48,7 @@ u64 = ctypes.c_uint64
 
 
 AFFINE_ROT_IDENTITY = 1
+AFFINE_ROT_Y = 2
 
 
 class Affine(ctypes.Structure):

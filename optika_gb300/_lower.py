@@ -43,7 +43,12 @@ def set_affine(dst: L.Affine, m: np.ndarray) -> None:
         hi, lo = split_f64(float(t[i]))
         dst.t_hi[i] = hi
         dst.t_lo[i] = lo
-    dst.flags = L.AFFINE_ROT_IDENTITY if np.array_equal(r, np.eye(3)) else 0
+    if np.array_equal(r, np.eye(3)):
+        dst.flags = L.AFFINE_ROT_IDENTITY
+    elif r[1, 1] == 1.0 and r[0, 1] == r[2, 1] == r[1, 0] == r[1, 2] == 0.0:
+        dst.flags = L.AFFINE_ROT_Y  # a rotation in the x-z plane
+    else:
+        dst.flags = 0
 
 
 @dataclasses.dataclass(eq=False)

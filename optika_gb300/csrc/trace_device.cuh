@@ -144,11 +144,28 @@ __device__ __forceinline__ void rot_row_ff(const float* mh, const float* ml, flo
   lo = l - (hi - s2);
 }
 
+// a x + b z in float-float for float-float entries (a, b) and vector
+// components (x, z): one row of a rotation in a coordinate plane.
+__device__ __forceinline__ void rot2_ff(float ah, float al, float bh, float bl, float x, float z,
+                                        float xl, float zl, float& hi, float& lo) {
+  const float p1 = ah * x, e1 = fmaf(ah, x, -p1);
+  const float p2 = bh * z, e2 = fmaf(bh, z, -p2);
+  float s, t;
+  two_sum(p1, p2, s, t);
+  float l = t + (e1 + e2);
+  l = fmaf(al, x, fmaf(bl, z, l));
+  l = fmaf(ah, xl, fmaf(bh, zl, l));
+  hi = s + l;
+  lo = l - (hi - s);
+}
+
 // Frame change of a ray: position (x, y, z) -> (x, y, z) + lo in the new
 // frame, direction (float-float) rotated.  Pure translations (the common
 // case) add the translation only; rotations are compensated, because an
 // FP32-rounded direction component (~3e-8 for 0.7) would act over the
-// whole incoming segment (hundreds of mm) before the intercept.
+// whole incoming segment (hundreds of mm) before the intercept.  A
+// rotation about y (tilts in the x-z plane: folds, tilted sensors and
+// gratings) mixes x and z only, with two-term rows; y passes through.
 __device__ __forceinline__ void frame_change(const otx_affine& f, Ray& r, float lo[3]) {
   float px = r.px, py = r.py, pz = r.pz;
   float rh[3], rl[3];
@@ -157,6 +174,18 @@ __device__ __forceinline__ void frame_change(const otx_affine& f, Ray& r, float 
     rh[1] = py;
     rh[2] = pz;
     rl[0] = rl[1] = rl[2] = 0.f;
+  } else if (f.flags & OTX_AFFINE_ROT_Y) {
+    rot2_ff(f.m[0], f.m_lo[0], f.m[2], f.m_lo[2], px, pz, 0.f, 0.f, rh[0], rl[0]);
+    rot2_ff(f.m[6], f.m_lo[6], f.m[8], f.m_lo[8], px, pz, 0.f, 0.f, rh[2], rl[2]);
+    rh[1] = py;
+    rl[1] = 0.f;
+    float dxh, dxl, dzh, dzl;
+    rot2_ff(f.m[0], f.m_lo[0], f.m[2], f.m_lo[2], r.dx, r.dz, r.lx, r.lz, dxh, dxl);
+    rot2_ff(f.m[6], f.m_lo[6], f.m[8], f.m_lo[8], r.dx, r.dz, r.lx, r.lz, dzh, dzl);
+    r.dx = dxh;
+    r.lx = dxl;
+    r.dz = dzh;
+    r.lz = dzl;
   } else {
     for (int i = 0; i < 3; ++i)
       rot_row_ff(f.m + 3 * i, f.m_lo + 3 * i, px, py, pz, 0.f, 0.f, 0.f, rh[i], rl[i]);
