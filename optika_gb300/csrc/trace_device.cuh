@@ -273,7 +273,7 @@ __device__ __forceinline__ float newton_step(int sag_type, const otx_surface& s,
   const float zs = sag_eval(sag_type, s, x, y, gx, gy);
   const float f = z - zs;
   const float fp = uz - (gx * ux + gy * uy);
-  const float dt = f / fp;
+  const float dt = __fdividef(f, fp);  // a small correction: 2 ulp of it suffice
   x = fmaf(-dt, ux, x);
   y = fmaf(-dt, uy, y);
   z = fmaf(-dt, uz, z);
@@ -314,7 +314,9 @@ __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
                                            float& x, float& y, float& z, float& tl) {
   const float oxf = ox + lo[0], oyf = oy + lo[1], ozf = oz + lo[2];
   if (sag_type == OTX_SAG_FLAT) {
-    const float inv = 1.f / uz;
+    // an approximate reciprocal: the Newton step below uses the same one,
+    // so the point lands on z = 0 and t + tl stays exact to rounding
+    const float inv = __fdividef(1.f, uz);
     const float t0 = -ozf * inv;
     const float t = t0 - (t0 * lz) * inv;  // first order in u_lo
     x = fmaf(t, ux, ox) + fmaf(t, lx, lo[0]);
@@ -338,8 +340,9 @@ __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
       const float q = sqrtf(fmaf(b, b, -cc));
       const float sg = sgnf(R * uz);
       // chosen root: -b - sg q ; the other root: -b + sg q ; product = cc
+      // (an approximate quotient: the Newton step polishes the root)
       if (sg != 0.f && sgnf(-b) == sg)
-        t = cc / (-b + sg * q);
+        t = __fdividef(cc, -b + sg * q);
       else
         t = -b - sg * q;
       break;
@@ -360,7 +363,8 @@ __device__ __forceinline__ float intercept(int sag_type, const otx_surface& s,
         tb = ta;
       } else {
         const float qq = -0.5f * (B + copysignf(sq, B));
-        const float r1 = qq / A, r2 = C / qq;
+        // approximate quotients: the Newton step polishes the chosen root
+        const float r1 = __fdividef(qq, A), r2 = __fdividef(C, qq);
         if (B >= 0.f) {
           ta = r1;
           tb = r2;
@@ -686,8 +690,9 @@ __device__ __forceinline__ void reflect_gradient(float& ax, float& ay, float& az
   float d_hi, d_lo;
   two_sum(1.f, q, d_hi, d_lo);
   d_lo += eq + (e1 + e2);
-  // k = 2 (a.v) / (v.v) as a float-float pair
-  const float inv = 1.f / d_hi;
+  // k = 2 (a.v) / (v.v) as a float-float pair; the correction term cancels
+  // the approximate reciprocal's error to second order
+  const float inv = __fdividef(1.f, d_hi);
   const float q_hi = n_hi * inv;
   const float rem = (fmaf(-q_hi, d_hi, n_hi) + n_lo) - q_hi * d_lo;
   const float k_hi = 2.f * q_hi, k_lo = 2.f * (rem * inv);
@@ -1030,7 +1035,9 @@ __device__ __forceinline__ void cm_normalize(cm2& m, int& exp2) {
   exp2 += e;
 }
 
-// Complex index of a layer at a vacuum wavelength (nm).
+// Complex index of a layer at a vacuum wavelength (nm).  FAST takes the
+// interpolation weight from an approximate quotient (2 ulp).
+template <bool FAST = false>
 __device__ __forceinline__ cf layer_n(const otx_system& sys, const otx_layer& L,
                                       float wl) {
   if (L.table < 0) return cf{L.n_re, L.n_im};
@@ -1050,7 +1057,8 @@ __device__ __forceinline__ cf layer_n(const otx_system& sys, const otx_layer& L,
     else
       hi = mid;
   }
-  const float w = (wl - xs[lo]) / (xs[hi] - xs[lo]);
+  const float w = FAST ? __fdividef(wl - xs[lo], xs[hi] - xs[lo])
+                       : (wl - xs[lo]) / (xs[hi] - xs[lo]);
   return cf{fmaf(w, ns[hi] - ns[lo], ns[lo]), fmaf(w, ks[hi] - ks[lo], ks[lo])};
 }
 
@@ -1111,9 +1119,11 @@ struct MLState {
 // q of the medium of index nj, from the Snell invariant:
 // cos_j = sqrt(1 - (n0 sin0)^2 / n_j^2) equals the reference's chained
 // optika/materials/_snells_law.py:13-38.
+template <bool FAST = false>
 __device__ __forceinline__ cf medium_q(const cf& inv0, const cf& nj, bool pol_p) {
   const cf nj2 = cmul(nj, nj);
-  const cf ratio = cscale(cmul(inv0, cconj(nj2)), 1.f / cabs2(nj2));
+  const float r = FAST ? __fdividef(1.f, cabs2(nj2)) : 1.f / cabs2(nj2);
+  const cf ratio = cscale(cmul(inv0, cconj(nj2)), r);
   const cf cj = csqrt(cf{1.f - ratio.re, -ratio.im});
   const cf w = cmul(nj, cj);
   return pol_p ? cscale(cconj(w), 1.f / cabs2(nj)) : w;
@@ -1312,10 +1322,12 @@ __device__ __forceinline__ bool stack_has_layers(const otx_stack& K) {
 __device__ __forceinline__ float fresnel_efficiency(const otx_system& sys, const otx_stack& K,
                                                     bool mirror, float wl, float cos0, cf n0) {
   cf n1{1.f, 0.f};
-  if (K.substrate >= 0) n1 = layer_n(sys, sys.layers[K.substrate], wl);
+  if (K.substrate >= 0) n1 = mirror ? layer_n<true>(sys, sys.layers[K.substrate], wl)
+                                    : layer_n(sys, sys.layers[K.substrate], wl);
   const cf inv0 = cscale(cmul(n0, n0), fmaf(-cos0, cos0, 1.f));
   if (mirror) {
-    const cf w = medium_q(inv0, n1, false);
+    // approximate quotients: R is wanted to ~1e-6, each adds ~2e-7
+    const cf w = medium_q<true>(inv0, n1, false);
     const cf q0 = cscale(n0, cos0);
     const float ns = cabs2(csub(q0, w)), ds = cabs2(cadd(q0, w));
     const cf a = cscale(q0, cabs2(n1)), b = cscale(w, cabs2(n0));
