@@ -102,7 +102,8 @@ static otx_status launch_trace(const otx_system* sys_in, int mode, const TraceAr
   otx_system local = *sys_in;
   fill_sensor(local.sensor);
   const otx_system* sys = &local;
-  int rpt = (launch && launch->rays_per_thread > 0) ? launch->rays_per_thread : 1;
+  const int rpt_req = launch ? launch->rays_per_thread : 0;  // 0: the library's choice
+  int rpt = rpt_req > 0 ? rpt_req : 1;
   if (rpt != 1 && rpt != 2) return OTX_ERR_INVALID;
   int block = (launch && launch->block_size > 0) ? launch->block_size : 256;
   if (block > 256 || block % 32 != 0) return OTX_ERR_INVALID;
@@ -121,7 +122,8 @@ static otx_status launch_trace(const otx_system* sys_in, int mode, const TraceAr
       if (stack_needs_product(*sys, sys->stacks[s.mat_stack])) ml = true;
     }
   }
-  if (!(launch && launch->generic_only) && launch_fixed(mode, acc, rpt, grid, block, *sys, a, st))
+  if (!(launch && launch->generic_only) &&
+      launch_fixed(mode, acc, rpt_req > 0 ? rpt_req : 0, grid, block, *sys, a, st))
     return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
   switch (mode) {
     case OTX_INPUT_RAYS:

@@ -147,3 +147,26 @@ def test_intensity(case):
     m = exact["unvignetted"]
     rel = np.abs(out["intensity"][m] - exact["intensity"][m]) / exact["intensity"][m]
     assert rel.max() <= INTENSITY_RTOL
+
+
+def test_packed_pair_kernel_agrees_with_one_ray_kernel(case):
+    """The two-rays-per-thread kernel on packed FP32 instructions
+    (otx_launch.rays_per_thread = 2) traces the same rays as the default
+    one-ray kernel to FP32 rounding, and is held to the same error budget."""
+    from optika_gb300 import _lib
+
+    system, g, out, counts, exact, _ = case
+    launch = _lib.Launch()
+    launch.rays_per_thread = 2
+    V2 = ok.vectors.Cartesian2dVectorArray
+    res = system.rayfunction(wavelength=g["wavelength"], field=V2(g["field_x"], g["field_y"]),
+                             pupil=V2(g["pupil_x"], g["pupil_y"]), normalized_field=False,
+                             normalized_pupil=False, image=True, launch=launch)
+    torch.cuda.synchronize()
+    pair = res.outputs.numpy()
+    m = exact["unvignetted"]
+    assert np.array_equal(pair["unvignetted"], m)
+    assert _pos_err(pair, out, m).max() <= 2e-6
+    assert _pos_err(pair, exact, m).max() <= POS_MEASURED_BOUND
+    assert np.abs(pair["opl"][m] - exact["opl"][m]).max() <= OPL_BOUND
+    assert int(res.image[0].sum()) == int(counts.sum())
