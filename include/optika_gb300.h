@@ -94,6 +94,7 @@ typedef int32_t otx_status;
 #define OTX_AFFINE_ROT_IDENTITY 1 /* m is exactly the identity           */
 #define OTX_AFFINE_ROT_Y 2        /* m is a rotation about y: its middle   */
                                   /* row and column are exactly (0, 1, 0) */
+#define OTX_AFFINE_IDENTITY 4     /* the whole map is exactly the identity */
 typedef struct otx_affine {
   float m[9];    /* row-major 3x3 rotation, high parts */
   float m_lo[9]; /* low parts                          */

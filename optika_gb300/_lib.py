@@ -49,6 +49,7 @@ u64 = ctypes.c_uint64
 
 AFFINE_ROT_IDENTITY = 1
 AFFINE_ROT_Y = 2
+AFFINE_IDENTITY = 4
 
 
 class Affine(ctypes.Structure):

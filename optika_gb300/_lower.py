@@ -45,6 +45,8 @@ def set_affine(dst: L.Affine, m: np.ndarray) -> None:
         dst.t_lo[i] = lo
     if np.array_equal(r, np.eye(3)):
         dst.flags = L.AFFINE_ROT_IDENTITY
+        if not np.any(t):
+            dst.flags |= L.AFFINE_IDENTITY
     elif r[1, 1] == 1.0 and r[0, 1] == r[2, 1] == r[1, 0] == r[1, 2] == 0.0:
         dst.flags = L.AFFINE_ROT_Y  # a rotation in the x-z plane
     else:

@@ -118,6 +118,7 @@ __device__ __forceinline__ void rotate(const otx_affine& f, float& x, float& y,
 __device__ __forceinline__ void affine_point_folded(const otx_affine& f,
                                                     float& x, float& y,
                                                     float& z) {
+  if (f.flags & OTX_AFFINE_IDENTITY) return;
   float lo[3];
   affine_point(f, x, y, z, lo);
   x += lo[0];
@@ -213,6 +214,10 @@ __device__ __forceinline__ void frame_change(const otx_affine& f, Ray& r, float 
 // Sag z(x, y) and its gradient for the curved sag types.
 // Conic: optika/sags/_conic.py:31-48 (sag), :50-75 (gradient c x / g).
 // Toroid: optika/sags/_toroidal.py:38-57 (sag), :59-88 (gradient).
+// FAST_GRAD forms the gradient's quotients approximately (2 ulp), for
+// Newton steps, whose root the gradient does not move; the sag value and
+// the normals keep exact quotients.
+template <bool FAST_GRAD = false>
 __device__ __forceinline__ float sag_eval(int sag_type, const otx_surface& s, float x,
                                           float y, float& gx, float& gy) {
   switch (sag_type) {
@@ -228,7 +233,7 @@ __device__ __forceinline__ float sag_eval(int sag_type, const otx_surface& s, fl
         return 0.5f * (c * r2);
       }
       const float g = sqrtf(1.f - kp1 * c * c * r2);
-      const float cg = c / g;
+      const float cg = FAST_GRAD ? __fdividef(c, g) : c / g;
       gx = cg * x;
       gy = cg * y;
       return c * r2 / (1.f + g);
@@ -250,9 +255,9 @@ __device__ __forceinline__ float sag_eval(int sag_type, const otx_surface& s, fl
       const float zy = c * y2 / (1.f + g);
       const float rz = r - zy;
       const float f = sqrtf(fmaf(rz, rz, -x * x));
-      const float inv_f = 1.f / f;
+      const float inv_f = FAST_GRAD ? __fdividef(1.f, f) : 1.f / f;
       gx = x * inv_f;
-      gy = rz * (c * y / g) * inv_f;
+      gy = rz * (FAST_GRAD ? __fdividef(c * y, g) : c * y / g) * inv_f;
       // r - f = (r^2 - f^2) / (r + f) = (z_y (2 r - z_y) + x^2) / (r + f),
       // free of the cancellation of r - f when f ~ r > 0
       if (r >= 0.f) return fmaf(zy, 2.f * r - zy, x * x) / (r + f);
@@ -270,7 +275,7 @@ __device__ __forceinline__ float newton_step(int sag_type, const otx_surface& s,
                                              float& y, float& z, float ux,
                                              float uy, float uz) {
   float gx, gy;
-  const float zs = sag_eval(sag_type, s, x, y, gx, gy);
+  const float zs = sag_eval<true>(sag_type, s, x, y, gx, gy);
   const float f = z - zs;
   const float fp = uz - (gx * ux + gy * uy);
   const float dt = __fdividef(f, fp);  // a small correction: 2 ulp of it suffice
