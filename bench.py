@@ -1015,6 +1015,22 @@ def main() -> None:
                 "peak_kind": "nominal at the measured maximum SM clock",
                 "executed_fp32_flops_per_ray_ncu": pj.get("flops_per_ray"),
                 "fma_pipe_active_pct_ncu": pj.get("fma_pipe_active_pct")}
+        if pj.get("warp_instructions_per_32_rays"):
+            # the resource the kernel is bound by: instruction issue, one warp
+            # instruction per cycle per scheduler (152 SMs x 4) at the
+            # measured maximum clock, against the ncu-counted instructions
+            # of this kernel per ray at its measured rate
+            wi = pj["warp_instructions_per_32_rays"] / 32.0
+            issue_peak = 152 * 4 * float(pk.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+            ach_i = wi * n / (kernel_ms * 1e-3) / 1e12
+            roofline["issue"] = {
+                "achieved": ach_i, "peak": issue_peak, "unit": "T warp-instructions/s",
+                "frac": ach_i / issue_peak, "warp_instructions_per_ray_ncu": wi,
+                "peak_kind": "nominal at the measured maximum SM clock",
+                "note": "the binding resource: at full issue this instruction count "
+                        "would put roofline.fp32 at " +
+                        f"{roofline['fp32']['frac'] / (ach_i / issue_peak):.2f}"
+                        if "fp32" in roofline else ""}
 
     cpu = None
     errors = None

@@ -626,6 +626,18 @@ typedef struct otx_cells {
 otx_status otx_cell_rays(const otx_cells* cells, int64_t first, int64_t count,
                          const otx_grid* out, void* stream);
 
+/* Cells [first, first + count) traced with their rays generated in the
+ * trace kernel (the rays of otx_cell_rays, never written to memory) and
+ * binned into `image` (required: it is the only output).  Replaces, fused,
+ * the cell sampling of SequentialSystem._rayfunction_from_vertices
+ * (optika/systems/_sequential.py:1002-1086) and the rayfunction and
+ * sensor.measure calls of SequentialSystem.image (:1088-1206).  The
+ * system's input_mode (grid at infinity or finite) tells how a cell's
+ * field and pupil coordinates make its ray. */
+otx_status otx_trace_cells(const otx_system* sys, const otx_cells* cells, int64_t first,
+                           int64_t count, const otx_image* image, const otx_launch* launch,
+                           void* stream);
+
 /* Detector exposure of an ideal sensor (optika/sensors/_sensors.py:173-252
  * expose; optika/sensors/materials/_materials.py:1576-1598 signal):
  * electrons[i] = Poisson(scale photons[i]) + read_noise N(0, 1) when

@@ -394,6 +394,8 @@ def _declare(lib: ctypes.CDLL) -> None:
     lib.otx_trace_batch_noalloc.restype = i32
     lib.otx_stop_newton.argtypes = [P(System), P(System), P(StopSolve), v]
     lib.otx_stop_newton.restype = i32
+    lib.otx_trace_cells.argtypes = [P(System), P(Cells), i64, i64, P(Image), P(Launch), v]
+    lib.otx_trace_cells.restype = i32
     lib.otx_gemm_bf16.argtypes = [v, i32, v, i32, i32, i32, i32, v, i32, v, i32, v, v, i32, v, v]
     lib.otx_gemm_bf16.restype = i32
     lib.otx_silu_backward.argtypes = [v, v, v, i64, v]

@@ -7,6 +7,7 @@
 #include <mutex>
 
 #include "../../include/optika_gb300.h"
+#include "cells.cuh"
 #include "trace_kernel_decl.h"
 
 namespace otx {
@@ -134,6 +135,12 @@ static otx_status launch_trace(const otx_system* sys_in, int mode, const TraceAr
       break;
     case OTX_INPUT_GRID_FINITE:
       launch_mode<OTX_INPUT_GRID_FINITE>(rpt, acc, ml, grid, block, *sys, a, st);
+      break;
+    case OTX_MODE_CELLS_INFINITY:
+      launch_mode<OTX_MODE_CELLS_INFINITY>(rpt, acc, ml, grid, block, *sys, a, st);
+      break;
+    case OTX_MODE_CELLS_FINITE:
+      launch_mode<OTX_MODE_CELLS_FINITE>(rpt, acc, ml, grid, block, *sys, a, st);
       break;
     default:
       return OTX_ERR_INVALID;
@@ -511,6 +518,33 @@ otx_status otx_trace_rays(const otx_system* sys, const otx_rays* in, const otx_r
   if (image) a.img = *image;
   a.count = in->count;
   return launch_trace(sys, OTX_INPUT_RAYS, a, launch, stream);
+}
+
+otx_status otx_trace_cells(const otx_system* sys, const otx_cells* cells, int64_t first,
+                           int64_t count, const otx_image* image, const otx_launch* launch,
+                           void* stream) {
+  otx_status st = validate_system(sys);
+  if (st != OTX_OK) return st;
+  if (sys->input_mode != OTX_INPUT_GRID_INFINITY && sys->input_mode != OTX_INPUT_GRID_FINITE)
+    return OTX_ERR_INVALID;
+  st = validate_cells(cells, first, count);
+  if (st != OTX_OK) return st;
+  if (!image || !image_any(*image)) return OTX_ERR_INVALID;  // the image is the output
+  st = validate_image(sys, image);
+  if (st != OTX_OK) return st;
+  if (launch && launch->accumulate) return OTX_ERR_INVALID;
+  const otx_cells& c = *cells;
+  const int64_t total = (int64_t)c.nw * c.nfx * c.nfy * c.npx * c.npy;
+  TraceArgs a;
+  memset(&a, 0, sizeof(a));
+  a.img = *image;
+  a.count = count;
+  a.cells = c;
+  a.first = first;
+  a.cells_idx32 = total <= (int64_t)UINT32_MAX ? 1 : 0;
+  const int mode = sys->input_mode == OTX_INPUT_GRID_INFINITY ? OTX_MODE_CELLS_INFINITY
+                                                              : OTX_MODE_CELLS_FINITE;
+  return launch_trace(sys, mode, a, launch, stream);
 }
 
 otx_status otx_trace_grid(const otx_system* sys, const otx_grid* in, const otx_rays* out,

@@ -28,7 +28,17 @@ bool try_pair(int grid, int block, const otx_system& sys, const TraceArgs& a, cu
 // and 1 the one-ray kernels, which measured faster.
 bool launch_fixed(int mode, bool acc, int rpt, int grid, int block, const otx_system& sys,
                   const TraceArgs& a, cudaStream_t st) {
-  if (mode != OTX_INPUT_GRID_INFINITY || acc) return false;
+  if (acc) return false;
+  if (mode == OTX_MODE_CELLS_INFINITY && rpt != 2) {
+    // the forward model's cells, their rays generated in the kernel
+    constexpr int C = OTX_MODE_CELLS_INFINITY;
+    if (try_fixed<C, Object, Stop, ConicMirror, FlatMirror, Detector>(grid, block, sys, a, st))
+      return true;
+    if (try_fixed<C, Object, Stop, ConicCoated, FlatCoated, Detector>(grid, block, sys, a, st))
+      return true;
+    return false;
+  }
+  if (mode != OTX_INPUT_GRID_INFINITY) return false;
   if (rpt == 2) {
     if (try_pair<Object, Stop, ConicMirror, FlatMirror, Detector>(grid, block, sys, a, st))
       return true;

@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include "../../include/optika_gb300.h"
+#include "cells.cuh"
 #include "trace_device.cuh"
 #include "trace_kernel_decl.h"
 
@@ -84,13 +85,24 @@ __device__ __forceinline__ void load_ray(const TraceArgs& a, int64_t i, Ray& r) 
     r.opl_hi = (float)o;
     r.opl_lo = (float)(o - (double)r.opl_hi);
   } else {
-    const otx_grid& g = a.grid;
-    const float wl = reinterpret_cast<const float*>(g.wavelength)[i * g.stride_wavelength];
-    const float fx = reinterpret_cast<const float*>(g.field_x)[i * g.stride_field];
-    const float fy = reinterpret_cast<const float*>(g.field_y)[i * g.stride_field];
-    const float qx = reinterpret_cast<const float*>(g.pupil_x)[i * g.stride_pupil];
-    const float qy = reinterpret_cast<const float*>(g.pupil_y)[i * g.stride_pupil];
-    if (MODE == OTX_INPUT_GRID_INFINITY) {
+    float wl, fx, fy, qx, qy;
+    float inten = 1.f;
+    if constexpr (MODE == OTX_MODE_CELLS_INFINITY || MODE == OTX_MODE_CELLS_FINITE) {
+      // the cell's ray, generated in place of reading a grid
+      if (a.cells_idx32)
+        cell_ray<uint32_t>(a.cells, a.first + i, wl, fx, fy, qx, qy, inten);
+      else
+        cell_ray<uint64_t>(a.cells, a.first + i, wl, fx, fy, qx, qy, inten);
+    } else {
+      const otx_grid& g = a.grid;
+      wl = reinterpret_cast<const float*>(g.wavelength)[i * g.stride_wavelength];
+      fx = reinterpret_cast<const float*>(g.field_x)[i * g.stride_field];
+      fy = reinterpret_cast<const float*>(g.field_y)[i * g.stride_field];
+      qx = reinterpret_cast<const float*>(g.pupil_x)[i * g.stride_pupil];
+      qy = reinterpret_cast<const float*>(g.pupil_y)[i * g.stride_pupil];
+      if (g.intensity) inten = reinterpret_cast<const float*>(g.intensity)[i * g.stride_intensity];
+    }
+    if (MODE == OTX_INPUT_GRID_INFINITY || MODE == OTX_MODE_CELLS_INFINITY) {
       r.px = qx;
       r.py = qy;
       direction_from_angles(fx, fy, r.dx, r.dy, r.dz, r.lx, r.ly, r.lz);
@@ -101,7 +113,7 @@ __device__ __forceinline__ void load_ray(const TraceArgs& a, int64_t i, Ray& r) 
     }
     r.pz = 0.f;
     r.wl = wl;
-    r.inten = g.intensity ? reinterpret_cast<const float*>(g.intensity)[i * g.stride_intensity] : 1.f;
+    r.inten = inten;
     r.att = 0.f;
     r.n = 1.f;
     r.ok = true;
@@ -296,6 +308,7 @@ __device__ __forceinline__ void propagate_fixed(const otx_system& sys, Ray& r) {
 // (unit) direction and nothing clips: the step is an exact no-op.
 template <int MODE, class K>
 __device__ __forceinline__ bool first_is_noop(const otx_system& sys) {
+  // (every mode but OTX_INPUT_RAYS starts its rays on the z = 0 plane)
   if constexpr (MODE != OTX_INPUT_RAYS && K::sag == OTX_SAG_FLAT && K::mat == OTX_MAT_VACUUM &&
                 K::aper == OTX_APER_NONE && K::rule == OTX_RULE_NONE) {
     const otx_affine& f = sys.surfaces[0].to_local;

@@ -28,12 +28,21 @@ __host__ __device__ __forceinline__ bool stack_needs_product(const otx_system& s
 // through it: type tags, pool indices and sizes (OTX_OK when usable).
 otx_status validate_system(const otx_system* sys);
 
+// Input modes of the trace kernels beyond the OTX_INPUT_* of a system:
+// scene cells whose rays the kernel generates itself (otx_trace_cells),
+// with the object at infinity or at a finite distance.
+#define OTX_MODE_CELLS_INFINITY 101
+#define OTX_MODE_CELLS_FINITE 102
+
 struct TraceArgs {
   otx_rays in;
   otx_grid grid;
   otx_rays out;
   otx_image img;
   int64_t count;
+  otx_cells cells;     // cell modes: the scene's tables
+  int64_t first;       // cell modes: cell index of ray 0
+  int32_t cells_idx32; // cell modes: every cell index fits 32 bits
 };
 
 template <int MODE>
@@ -46,6 +55,12 @@ extern template void launch_mode<OTX_INPUT_GRID_INFINITY>(int, bool, bool, int, 
                                                           const otx_system&,
                                                           const TraceArgs&, cudaStream_t);
 extern template void launch_mode<OTX_INPUT_GRID_FINITE>(int, bool, bool, int, int,
+                                                        const otx_system&,
+                                                        const TraceArgs&, cudaStream_t);
+extern template void launch_mode<OTX_MODE_CELLS_INFINITY>(int, bool, bool, int, int,
+                                                          const otx_system&,
+                                                          const TraceArgs&, cudaStream_t);
+extern template void launch_mode<OTX_MODE_CELLS_FINITE>(int, bool, bool, int, int,
                                                         const otx_system&,
                                                         const TraceArgs&, cudaStream_t);
 

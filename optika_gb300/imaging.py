@@ -159,12 +159,17 @@ def cell_tables(system, scene: FunctionArray, pupil=None, normalized_field: bool
 
 class ImagePlan:
     """An image simulation with its tables and device buffers made once:
-    :meth:`run` enqueues the chunks (cell rays, fused trace with binning)
-    and the exposure on the current stream and returns the electrons."""
+    :meth:`run` enqueues the trace of every cell with sensor binning and the
+    exposure on the current stream and returns the electrons.
+
+    ``fused`` (default): one launch generates each cell's ray inside the
+    trace kernel (otx_trace_cells), so no ray is written to memory.
+    ``fused=False``: chunks of ``chunk`` cells, each a cell-ray launch into
+    device buffers (otx_cell_rays) and a trace of those buffers."""
 
     def __init__(self, system, scene: FunctionArray, pupil=None, normalized_field: bool = True,
                  normalized_pupil: bool = True, integrate: bool = True, random: bool = True,
-                 seed: int = 0, chunk: int = 1 << 24):
+                 seed: int = 0, chunk: int = 1 << 24, fused: bool = True):
         from . import _api
 
         sensor = system.sensor
@@ -201,7 +206,9 @@ class ImagePlan:
         self.seed = int(seed)
         self.count = t.count
         self.chunk = max(1, min(int(chunk), self.count))
-        self._buf = [torch.empty(self.chunk, dtype=torch.float32, device=dev) for _ in range(6)]
+        self.fused = bool(fused)
+        nbuf = 1 if self.fused else self.chunk  # the fused trace reads no buffers
+        self._buf = [torch.empty(nbuf, dtype=torch.float32, device=dev) for _ in range(6)]
         b = self._buf
         self.trace = _api.PreparedTrace(
             system, wavelength=b[0], field=Cartesian2dVectorArray(b[1], b[2]),
@@ -210,14 +217,28 @@ class ImagePlan:
 
     @property
     def launches(self) -> int:
-        """Kernels per :meth:`run`: per chunk the cell rays and the trace,
-        then the exposure."""
+        """Kernels per :meth:`run`: the trace (fused) or, per chunk, the cell
+        rays and the trace; then the exposure."""
+        if self.fused:
+            return 2
         return 2 * ((self.count + self.chunk - 1) // self.chunk) + 1
 
     def photons(self) -> tuple[torch.Tensor, torch.Tensor]:
         """Photon image and flux-weighted cosine moment of the cells."""
+        import ctypes
+
         from . import _api
 
+        if self.fused:
+            t = self.trace
+            t.counts.zero_()
+            t.flux.zero_()
+            t.moment.zero_()
+            L.check(L.load().otx_trace_cells(
+                ctypes.byref(t.lowering.sys), ctypes.byref(self.cells), 0, self.count,
+                ctypes.byref(t.img), ctypes.byref(t.launch_desc), _api.stream_handle()),
+                "otx_trace_cells")
+            return t.flux, t.moment
         for first in range(0, self.count, self.chunk):
             n = min(self.chunk, self.count - first)
             self.trace.grid.count = n

@@ -202,6 +202,33 @@ def test_wavelength_bins_and_chunks(cuda):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("coated", [False, True])
+def test_fused_cell_trace_equals_cell_rays_then_trace(cuda, coated):
+    """otx_trace_cells (each cell's ray generated inside the trace kernel)
+    bins the same rays as otx_cell_rays into buffers followed by the trace
+    of those buffers in chunks: identical counts, flux to FP32 summation."""
+    import torch
+
+    from optika_gb300.imaging import ImagePlan
+
+    s = configs.newtonian(coated=coated)
+    scene = _scene(nw=3, nf=16)
+    kw = dict(normalized_field=False, normalized_pupil=False, integrate=False, random=True,
+              seed=9)
+    fused = ImagePlan(s, scene, _pupil(n=12), fused=True, **kw)
+    split = ImagePlan(s, scene, _pupil(n=12), fused=False, chunk=1000, **kw)
+    assert fused.launches == 2 and split.launches > 2
+    f_flux, f_mom = (t.clone() for t in fused.photons())
+    f_counts = fused.trace.counts.clone()
+    s_flux, s_mom = split.photons()
+    torch.cuda.synchronize()
+    assert f_counts.sum().item() > 0.5 * fused.count
+    assert torch.equal(f_counts, split.trace.counts)
+    assert torch.allclose(f_flux, s_flux, rtol=1e-5, atol=1e-6 * float(s_flux.max()))
+    assert torch.allclose(f_mom, s_mom, rtol=1e-5, atol=1e-6 * float(s_mom.max()))
+
+
+@pytest.mark.gpu
 def test_normalized_scene_fills_the_stops(cuda):
     """Normalised field and pupil vertices are denormalised per wavelength
     vertex by the stop solver: the image equals the one of the physical
