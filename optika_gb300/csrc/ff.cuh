@@ -30,11 +30,14 @@ __device__ __forceinline__ ff ff_twosum(float a, float b) {
 
 __device__ __forceinline__ ff ff_of(float a) { return ff{a, 0.f}; }
 
+// The double-word sum with one TwoSum (Joldes, Muller and Popescu 2017,
+// "sloppy" DWPlusDW): its error is within ~2^-47 of the larger operand,
+// not of the sum, which is all the transfer-matrix products need (their
+// entries are rescaled to O(1) and R, T are wanted to 1e-5 absolute); it
+// takes about half the instructions of the accurate form.
 __device__ __forceinline__ ff ff_add(ff a, ff b) {
   const ff s = ff_twosum(a.hi, b.hi);
-  const ff t = ff_twosum(a.lo, b.lo);
-  ff u = ff_fast2sum(s.hi, s.lo + t.hi);
-  return ff_fast2sum(u.hi, u.lo + t.lo);
+  return ff_fast2sum(s.hi, s.lo + (a.lo + b.lo));
 }
 
 __device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
