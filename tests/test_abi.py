@@ -268,3 +268,41 @@ def test_rulings_cells_expose_reduce_validation(built_library):
     assert lib.otx_pupil_reduce(ctypes.byref(rr), 2, 5, None, None) == L.ERR_INVALID
     assert lib.otx_pupil_reduce(ctypes.byref(rr), 0, 5, None, None) == L.OK
     assert lib.otx_pupil_reduce(ctypes.byref(rr), 2, 0, None, None) == L.ERR_INVALID
+
+
+def test_stop_newton_and_trace_cells_validation(built_library):
+    """The device stop solve and the fused cell trace reject bad arguments
+    on the host and return at once on empty inputs."""
+    lib = built_library
+    s = _system(2)
+    first = _system(1)
+    sol = L.StopSolve()
+    sol.max_iterations, sol.polish_steps, sol.step, sol.tolerance = 60, 2, 1e-4, 1e-9
+    call = lambda: lib.otx_stop_newton(ctypes.byref(s), ctypes.byref(first),  # noqa: E731
+                                       ctypes.byref(sol), None)
+    assert call() == L.OK  # count 0: no device work
+    assert lib.otx_stop_newton(None, ctypes.byref(first), ctypes.byref(sol), None) == L.ERR_INVALID
+    sol.count = 10
+    assert call() == L.ERR_INVALID  # arrays missing
+    for k in ("position", "direction", "wavelength", "target_x", "target_y", "status"):
+        setattr(sol, k, 256)
+    sol.tolerance = 0.0
+    assert call() == L.ERR_INVALID
+    sol.tolerance, sol.max_iterations = 1e-9, 0
+    assert call() == L.ERR_INVALID
+    # fused cell trace: the image is its output; cells checked as otx_cell_rays
+    c = L.Cells()
+    c.nw = c.nfx = c.nfy = c.npx = c.npy = 2
+    img = L.Image()
+    launch = L.Launch()
+    fn = lambda first_, count, image: lib.otx_trace_cells(  # noqa: E731
+        ctypes.byref(s), ctypes.byref(c), first_, count, image, ctypes.byref(launch), None)
+    assert fn(0, 4, ctypes.byref(img)) == L.ERR_INVALID  # no image buffer
+    img.counts = 256
+    s.sensor.num_x = s.sensor.num_y = s.sensor.num_w = 4
+    s.sensor.width_x = s.sensor.width_y = 0.01
+    assert fn(0, 0, ctypes.byref(img)) == L.OK  # empty: no device work
+    assert fn(30, 3, ctypes.byref(img)) == L.ERR_SIZE  # past the last cell
+    assert fn(0, 8, ctypes.byref(img)) == L.ERR_INVALID  # tables missing
+    s.input_mode = L.INPUT_RAYS
+    assert fn(0, 0, ctypes.byref(img)) == L.ERR_INVALID  # grid systems only
