@@ -106,7 +106,7 @@ def _to_ray_array(b: dict, shape: tuple) -> RayVectorArray:
         intensity=rs(b["intensity"]),
         attenuation=rs(b["attenuation"]),
         index_refraction=rs(b["index_refraction"]),
-        unvignetted=rs(b["unvignetted"]).bool(),
+        unvignetted=rs(b["unvignetted"]).view(torch.bool),  # bytes 0 / 1: a view, no copy
         opl=rs(b["opl"]),
     )
 
@@ -236,7 +236,7 @@ def _to_ray_array_partial(b: dict, shape: tuple) -> RayVectorArray:
         intensity=rs(b["intensity"]),
         attenuation=rs(b["attenuation"]),
         index_refraction=rs(b["index_refraction"]),
-        unvignetted=None if unv is None else unv.bool(),
+        unvignetted=None if unv is None else unv.view(torch.bool),
         opl=rs(b["opl"]),
     )
 

@@ -134,6 +134,28 @@ __device__ __forceinline__ cmff cmff_mul(const cmff& x, const cmff& y) {
               cff_add(cff_mul(x.c, y.b), cff_mul(x.d, y.d))};
 }
 
+// x^2 of a complex float-float: (re^2 - im^2, 2 re im).
+__device__ __forceinline__ cff cff_sqr(cff a) {
+  return cff{ff_sub(ff_mul(a.re, a.re), ff_mul(a.im, a.im)), ff_scale2(ff_mul(a.re, a.im), 2.f)};
+}
+
+// M^2 of a 2x2 matrix: [[a^2 + bc, b (a + d)], [c (a + d), d^2 + bc]].
+__device__ __forceinline__ cmff cmff_sqr(const cmff& m) {
+  const cff bc = cff_mul(m.b, m.c), tr = cff_add(m.a, m.d);
+  return cmff{cff_add(cff_sqr(m.a), bc), cff_mul(m.b, tr), cff_mul(m.c, tr),
+              cff_add(cff_sqr(m.d), bc)};
+}
+
+// A column vector of two complex float-float values.
+struct cvff {
+  cff x, y;
+};
+
+__device__ __forceinline__ cvff cmff_apply(const cmff& m, const cvff& v) {
+  return cvff{cff_add(cff_mul(m.a, v.x), cff_mul(m.b, v.y)),
+              cff_add(cff_mul(m.c, v.x), cff_mul(m.d, v.y))};
+}
+
 // Exact power-of-two rescaling so the largest component is O(1).
 __device__ __forceinline__ void cmff_normalize(cmff& m, int& exp2) {
   const float mx = fmaxf(fmaxf(fmaxf(fabsf(m.a.re.hi), fabsf(m.a.im.hi)),
@@ -147,6 +169,17 @@ __device__ __forceinline__ void cmff_normalize(cmff& m, int& exp2) {
   m.b = cff_scale2(m.b, s);
   m.c = cff_scale2(m.c, s);
   m.d = cff_scale2(m.d, s);
+  exp2 += e;
+}
+
+__device__ __forceinline__ void cvff_normalize(cvff& v, int& exp2) {
+  const float mx = fmaxf(fmaxf(fabsf(v.x.re.hi), fabsf(v.x.im.hi)),
+                         fmaxf(fabsf(v.y.re.hi), fabsf(v.y.im.hi)));
+  if (!(mx > 0.f) || !isfinite(mx)) return;
+  const int e = ilogbf(mx);
+  const float s = ldexpf(1.f, -e);
+  v.x = cff_scale2(v.x, s);
+  v.y = cff_scale2(v.y, s);
   exp2 += e;
 }
 

@@ -21,41 +21,68 @@ __device__ __forceinline__ ff ff_2pi() { return ff{6.28318548202514648f, -1.7484
 __device__ __forceinline__ ff ff_pio2() { return ff{1.57079637050628662f, -4.37113883e-08f}; }
 __device__ __forceinline__ ff ff_ln2() { return ff{0.693147182464599609f, -1.90465421e-09f}; }
 
+// Taylor coefficients as float-float pairs (hi + lo): 1/i! for exp,
+// (-1)^k/(2k+1)! for sin, (-1)^k/(2k)! for cos, each exact to ~2^-72.
+__device__ __forceinline__ ff ffc(float hi, float lo) { return ff{hi, lo}; }
+
+// Horner step p r + c in float-float.
+__device__ __forceinline__ ff ff_horner(ff p, ff r, ff c) { return ff_add(ff_mul(p, r), c); }
+
 // exp(x) for a float-float x: x = k ln2 + r, |r| <= ln2 / 2, exp(r) by its
-// Taylor series to r^13 / 13!, then scaled by 2^k.
+// Taylor series to r^13 / 13! (Horner), then scaled by 2^k.  The terms from
+// r^8 on are below 2^-25 of the sum, so their part of the Horner scheme
+// runs in FP32; the rest runs in float-float.
 __device__ __forceinline__ ff ff_exp(ff x) {
   if (x.hi > 88.f) return ff{INFINITY, 0.f};
   if (x.hi < -103.f) return ff{0.f, 0.f};
   const float k = rintf(x.hi * 1.44269504088896341f);
   const ff r = ff_sub(x, ff_mulf(ff_ln2(), k));
-  ff term = ff_of(1.f), sum = ff_of(1.f);
-#pragma unroll
-  for (int i = 1; i <= 13; ++i) {
-    term = ff_div(ff_mul(term, r), ff_of((float)i));  // r^i / i!
-    sum = ff_add(sum, term);
-  }
-  return ff_scale2(sum, ldexpf(1.f, (int)k));
+  const float rf = r.hi;
+  float t = fmaf(0x1.612462p-33f, rf, 0x1.1eed8ep-29f);  // 1/13!, 1/12!
+  t = fmaf(t, rf, 0x1.ae6456p-26f);                      // 1/11!
+  t = fmaf(t, rf, 0x1.27e4fcp-22f);                      // 1/10!
+  t = fmaf(t, rf, 0x1.71de3ap-19f);                      // 1/9!
+  t = fmaf(t, rf, 0x1.a01a02p-16f);                      // 1/8!
+  ff p = ff_add(ff_mul(ff_of(t), r), ffc(0x1.a01a02p-13f, -0x1.7f97fap-39f));  // 1/7!
+  p = ff_horner(p, r, ffc(0x1.6c16c2p-10f, -0x1.27d27ep-35f));                 // 1/6!
+  p = ff_horner(p, r, ffc(0x1.111112p-7f, -0x1.dddddep-32f));                  // 1/5!
+  p = ff_horner(p, r, ffc(0x1.555556p-5f, -0x1.555556p-30f));                  // 1/4!
+  p = ff_horner(p, r, ffc(0x1.555556p-3f, -0x1.555556p-28f));                  // 1/3!
+  p = ff_horner(p, r, ff_of(0.5f));
+  p = ff_horner(p, r, ff_of(1.f));
+  p = ff_horner(p, r, ff_of(1.f));
+  return ff_scale2(p, ldexpf(1.f, (int)k));
 }
 
 // sin and cos of a float-float x: x = k pi/2 + r, |r| <= pi/4, Taylor
-// series of sin(r), cos(r) to r^17, then the quadrant of k.
+// series of sin(r) to r^17 and cos(r) to r^16 (Horner in r^2), then the
+// quadrant of k.  The terms from r^10 (cos) and r^11 (sin) on are below
+// 2^-25 of the sum and run in FP32.
 __device__ __forceinline__ void ff_sincos(ff x, ff& s, ff& c) {
   const float k = rintf(x.hi * 0.636619772367581343f);
   const ff r = ff_sub(x, ff_mulf(ff_pio2(), k));
   const ff r2 = ff_mul(r, r);
-  // sin r = r (1 - r^2/(2*3) (1 - r^2/(4*5) (1 - ...)))  (Horner on the ratios)
-  ff ps = ff_of(1.f), pc = ff_of(1.f);
-#pragma unroll
-  for (int i = 8; i >= 1; --i) {
-    const ff rs = ff_div(r2, ff_of((float)((2 * i) * (2 * i + 1))));
-    const ff rc = ff_div(r2, ff_of((float)((2 * i - 1) * (2 * i))));
-    ps = ff_sub(ff_of(1.f), ff_mul(rs, ps));
-    pc = ff_sub(ff_of(1.f), ff_mul(rc, pc));
-  }
+  const float q = r2.hi;
+  float ts = fmaf(0x1.952c78p-49f, q, -0x1.ae7f3ep-41f);  // 1/17!, -1/15!
+  ts = fmaf(ts, q, 0x1.612462p-33f);                       // 1/13!
+  ts = fmaf(ts, q, -0x1.ae6456p-26f);                      // -1/11!
+  float tc = fmaf(0x1.ae7f3ep-45f, q, -0x1.93974ap-37f);  // 1/16!, -1/14!
+  tc = fmaf(tc, q, 0x1.1eed8ep-29f);                       // 1/12!
+  tc = fmaf(tc, q, -0x1.27e4fcp-22f);                      // -1/10!
+  ff ps = ff_add(ff_mul(ff_of(ts), r2), ffc(0x1.71de3ap-19f, 0x1.55b1ccp-45f));  // 1/9!
+  ff pc = ff_add(ff_mul(ff_of(tc), r2), ffc(0x1.a01a02p-16f, -0x1.7f97fap-42f));  // 1/8!
+  ps = ff_horner(ps, r2, ffc(-0x1.a01a02p-13f, 0x1.7f97fap-39f));  // -1/7!
+  pc = ff_horner(pc, r2, ffc(-0x1.6c16c2p-10f, 0x1.27d27ep-35f));  // -1/6!
+  ps = ff_horner(ps, r2, ffc(0x1.111112p-7f, -0x1.dddddep-32f));   // 1/5!
+  pc = ff_horner(pc, r2, ffc(0x1.555556p-5f, -0x1.555556p-30f));   // 1/4!
+  ps = ff_horner(ps, r2, ffc(-0x1.555556p-3f, 0x1.555556p-28f));   // -1/3!
+  pc = ff_horner(pc, r2, ff_of(-0.5f));
+  ps = ff_horner(ps, r2, ff_of(1.f));
+  pc = ff_horner(pc, r2, ff_of(1.f));
   const ff sr = ff_mul(r, ps);
   const ff cr = pc;
-  const int q = ((int)k) & 3;
-  switch (q) {
+  const int qd = ((int)k) & 3;
+  switch (qd) {
     case 0: s = sr; c = cr; break;
     case 1: s = cr; c = ff_neg(sr); break;
     case 2: s = ff_neg(sr); c = ff_neg(cr); break;
@@ -172,7 +199,7 @@ __device__ __forceinline__ void cmff_pow(cmff base, int bexp, int e, cmff& acc, 
     }
     e >>= 1;
     if (e) {
-      base = cmff_mul(base, base);
+      base = cmff_sqr(base);
       bexp *= 2;
       cmff_normalize(base, bexp);
     }
@@ -321,26 +348,6 @@ __device__ __forceinline__ LayerPhase layer_phase_ff(const cff& w, float thickne
   return L;
 }
 
-// One interface (and layer) step of the product, as layer_step_ff: the
-// matrix from the current medium q into qj, with the layer's propagation
-// when ph is given.
-__device__ __forceinline__ void bilayer_step(MLff& st, const cff& qj, const LayerPhase* ph) {
-  const cff a = cff_add(st.q, qj), b = cff_sub(st.q, qj);
-  cmff tm{a, b, b, a};
-  bool wprop = true;
-  if (ph) {
-    wprop = ph->prop;
-    if (wprop) tm = cmff{cff_mul(a, ph->em), cff_mul(b, ph->ep), cff_mul(b, ph->em), cff_mul(a, ph->ep)};
-  }
-  if (st.where) {
-    mlff_times(st, tm, 0);
-    st.t = ff_mul(st.t, ff_scale2(cff_abs2(st.q), 4.f));
-    ff_normalize_scalar(st.t, st.te);
-  }
-  st.where = st.where && wprop;
-  st.q = qj;
-}
-
 // t^e (e >= 1) for a normalised positive scalar, exponent tracked in te.
 __device__ __forceinline__ void ff_pow_scalar(ff t, int te, int e, ff& out, int& oute) {
   bool first = true;
@@ -365,57 +372,101 @@ __device__ __forceinline__ void ff_pow_scalar(ff t, int te, int e, ff& out, int&
   }
 }
 
+// The step matrix from the medium of factor q into qj through a layer of
+// phase ph (as layer_step_ff): [[a em, b ep], [b em, a ep]], a = q + qj,
+// b = q - qj.
+__device__ __forceinline__ cmff step_matrix(const cff& q, const cff& qj, const LayerPhase& ph) {
+  const cff a = cff_add(q, qj), b = cff_sub(q, qj);
+  return cmff{cff_mul(a, ph.em), cff_mul(b, ph.ep), cff_mul(b, ph.em), cff_mul(a, ph.ep)};
+}
+
+// The same step matrix applied to a column vector.
+__device__ __forceinline__ cvff step_apply(const cff& q, const cff& qj, const LayerPhase& ph,
+                                           const cvff& v) {
+  const cff a = cff_add(q, qj), b = cff_sub(q, qj);
+  const cff x = cff_mul(ph.em, v.x), y = cff_mul(ph.ep, v.y);
+  return cvff{cff_add(cff_mul(a, x), cff_mul(b, y)), cff_add(cff_mul(b, x), cff_mul(a, y))};
+}
+
+// First column of the step matrix of an interface alone: (q + qj, q - qj).
+__device__ __forceinline__ cvff step_column(const cff& q, const cff& qj) {
+  return cvff{cff_add(q, qj), cff_sub(q, qj)};
+}
+
+// The transmission factor's term 4 |q|^2 of a step out of the medium q.
+__device__ __forceinline__ void t_step(ff& t, int& te, const cff& q) {
+  t = ff_mul(t, ff_scale2(cff_abs2(q), 4.f));
+  ff_normalize_scalar(t, te);
+}
+
 // R and T of one polarisation of [A, B] x periods on a substrate, given the
-// media factors q0 (ambient), qa, qb, qs and the two layers' phases: the
-// steps and the period power of multilayer_pol_ff for a periodic stack,
-// with the transmission factor of the repeated periods raised by squaring.
+// media factors q0 (ambient), qa, qb, qs and the two layers' phases.  The
+// product of the step matrices, M = T1 T2 (T3 T4)^(periods - 1) Ts (first
+// period from the ambient, the repeated period from its own last medium,
+// then the substrate: multilayer_pol_ff's order), enters R = |M10 / M00|^2
+// and T only through its first column M e1, so it is evaluated from the
+// right as matrix-vector products: only the period matrix P = T3 T4 is
+// formed, and P^(periods - 1) is applied by squaring P.  A layer too opaque
+// to propagate through (|exp(-i beta)| >= 1e10) ends the product at its
+// interface and the stack transmits nothing, as in the sequential form.
 __device__ __forceinline__ void bilayer_pol_ff(const cff& q0, const cff& qa, const cff& qb,
                                                const cff& qs, const LayerPhase& A,
                                                const LayerPhase& B, int periods, float& R,
                                                float& T) {
-  MLff st;
-  st.e = 0;
-  st.first = true;
-  st.t = ff_of(1.f);
-  st.te = 0;
-  st.q = q0;
-  st.n = cf{1.f, 0.f};  // unused: the bilayer form has no interface profiles
-  st.where = true;
-  if (periods > 0) {
-    bilayer_step(st, qa, &A);  // first period
-    bilayer_step(st, qb, &B);
-    MLff per = st;
-    per.first = true;
-    per.e = 0;
-    per.t = ff_of(1.f);
-    per.te = 0;
-    bilayer_step(per, qa, &A);  // the period, from its own last medium
-    bilayer_step(per, qb, &B);
+  cvff u;
+  int ue = 0;
+  ff t = ff_of(1.f);
+  int te = 0;
+  bool where = true;
+  if (periods <= 0) {
+    u = step_column(q0, qs);
+    t_step(t, te, q0);
+  } else if (!A.prop) {
+    u = step_column(q0, qa);
+    where = false;
+  } else if (!B.prop) {
+    u = step_apply(q0, qa, A, step_column(qa, qb));
+    where = false;
+  } else {
+    u = step_column(qb, qs);  // Ts e1
     const int reps = periods - 1;
-    if (!per.first && reps > 0) {
-      cmff pm;
+    if (reps > 0) {
+      cmff P = cmff_mul(step_matrix(qb, qa, A), step_matrix(qa, qb, B));
       int pe = 0;
-      cmff_pow(per.m, per.e, reps, pm, pe);
-      mlff_times(st, pm, pe);
-      ff pt;
+      cmff_normalize(P, pe);
+      for (int e = reps;;) {
+        if (e & 1) {
+          u = cmff_apply(P, u);
+          ue += pe;
+          cvff_normalize(u, ue);
+        }
+        e >>= 1;
+        if (!e) break;
+        P = cmff_sqr(P);
+        pe *= 2;
+        cmff_normalize(P, pe);
+      }
+      ff pt = ff_of(1.f);
       int pte = 0;
-      ff_pow_scalar(per.t, per.te, reps, pt, pte);
-      st.t = ff_mul(st.t, pt);
-      st.te += pte;
-      ff_normalize_scalar(st.t, st.te);
+      t_step(pt, pte, qb);
+      t_step(pt, pte, qa);
+      ff_pow_scalar(pt, pte, reps, t, te);
     }
-    st.where = per.where;
-    st.q = per.q;
-    st.n = per.n;
+    u = step_apply(qa, qb, B, u);
+    cvff_normalize(u, ue);
+    u = step_apply(q0, qa, A, u);
+    cvff_normalize(u, ue);
+    t_step(t, te, q0);  // first period and substrate steps
+    t_step(t, te, qa);
+    t_step(t, te, qb);
   }
-  bilayer_step(st, qs, nullptr);  // into the substrate
-  const ff m11 = cff_abs2(st.m.a);
-  R = ff_to_f(ff_div(cff_abs2(st.m.c), m11));
+  const ff m11 = cff_abs2(u.x);
+  R = ff_to_f(ff_div(cff_abs2(u.y), m11));
   T = 0.f;
-  if (st.where) {
-    const ff ratio = cff_div(st.q, q0).re;
-    const ff tt = ff_mul(ff_div(st.t, m11), ratio);
-    T = ldexpf(ff_to_f(tt), st.te - 2 * st.e);
+  if (where) {
+    const ff ratio = cff_div(qs, q0).re;
+    const ff tt = ff_mul(ff_div(t, m11), ratio);
+    T = ldexpf(ff_to_f(tt), te - 2 * ue);
   }
 }
 
