@@ -243,6 +243,34 @@ def fp32_roofline(workload: str, units: int, ms: float, pk: dict) -> dict | None
             "peak_kind": "nominal at the measured maximum SM clock"}
 
 
+def issue_roofline(profile: str, units: int, ms: float, pk: dict, fp32: dict | None) -> dict | None:
+    """The instruction-issue roofline of a kernel: the warp instructions per
+    unit that ncu counted (profiles/<profile>.json) x units over the kernel's
+    time, against 152 SMs x 4 schedulers x one warp instruction per cycle at
+    the measured maximum SM clock."""
+    p = ROOT / "profiles" / f"{profile}.json"
+    if not p.exists():
+        return None
+    wi = float(json.loads(p.read_text())["warp_instructions_per_unit"])
+    peak = 152 * 4 * float(pk.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    ach = wi * units / (ms * 1e-3) / 1e12
+    out = {"achieved": ach, "peak": peak, "unit": "T warp-instructions/s", "frac": ach / peak,
+           "warp_instructions_per_unit_ncu": wi, "counted_in": f"profiles/{profile}.json",
+           "peak_kind": "nominal at the measured maximum SM clock"}
+    if fp32:
+        out["note"] = ("the binding resource: at full issue this instruction count would put "
+                       f"roofline.fp32 at {fp32['frac'] / (ach / peak):.2f}")
+    return out
+
+
+def _ncu_traffic(profile: str, units: int) -> float | None:
+    """DRAM bytes per launch of `units` units from a profile's ncu capture."""
+    p = ROOT / "profiles" / f"{profile}.json"
+    if not p.exists():
+        return None
+    return float(json.loads(p.read_text())["dram_bytes_per_unit"]) * units
+
+
 def run_reference(args, rank: int, world: int) -> None:
     if rank != 0:
         return
@@ -581,6 +609,7 @@ def run_multilayer(args, rank: int, world: int, emit: bool = True) -> dict:
     bps = 12 + 16  # wavelength, cosine, mirror index in; R_s, R_p, T_s, T_p out
     pk, pk_kind = peaks()
     ach = bps * n / (ms * 1e-3) / 1e9
+    fp32 = fp32_roofline("multilayer-periodic", n, ms, pk)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
@@ -597,12 +626,14 @@ def run_multilayer(args, rank: int, world: int, emit: bool = True) -> dict:
             "config": {"workload": "multilayer-periodic", "mirrors": 256, "samples": n,
                        "bilayers": 40, "l2": "inputs and outputs 280 MB, larger than L2"},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                         "frac": ach / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+                         "frac": ach / pk["hbm_gbs"],
+                         "traffic": _ncu_traffic("multilayer_periodic_1e7", n),
+                         "peak_kind": pk_kind,
                          "bytes_per_sample": bps, "kernel": "k_multilayer_periodic",
-                         "kernel_ms": ms,
-                         "fp32": fp32_roofline("multilayer-periodic", n, ms, pk),
-                         "note": "compute-bound (FP32 issue): the byte roofline is shown for "
-                                 "completeness"},
+                         "kernel_ms": ms, "fp32": fp32, "issue": issue_roofline(
+                             "multilayer_periodic_1e7", n, ms, pk, fp32),
+                         "note": "compute-bound (instruction issue): the byte roofline is "
+                                 "shown for completeness"},
             "cpu_baseline": cpu, "gpu_launches": args.steps, "clocks": clk,
     }
     if emit and rank == 0:

@@ -319,11 +319,13 @@ __device__ __forceinline__ bool first_is_noop(const otx_system& sys) {
   }
 }
 
-// The shape-specialised kernels keep 4 CTAs of 256 threads resident per SM
-// (at most 64 registers per thread): they are bound by instruction issue,
-// and 3 CTAs per SM lose ~9 % of it.
+// The shape-specialised kernels keep 6 CTAs of 256 threads resident per SM
+// (at most 40 registers per thread, no spills for the Newtonian shapes):
+// they are bound by instruction issue and latency, and measured on the
+// precision workload 6 CTAs per SM run 4 % faster than 4 (64 registers),
+// which run 9 % faster than 3; at 7 the registers spill.
 template <int MODE, class K0, class... Ks>
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256, 6)
     k_trace_fixed(const __grid_constant__ otx_system sys,
                   const __grid_constant__ TraceArgs a) {
   const int64_t n = a.count;
