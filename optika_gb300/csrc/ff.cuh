@@ -56,6 +56,41 @@ __device__ __forceinline__ ff ff_mulf(ff a, float b) {
   return ff_fast2sum(p, e);
 }
 
+// a b + c d in one pass: the two leading products and their exact errors
+// (FMA), one TwoSum of the products, the cross terms accumulated in FP32,
+// one Fast2Sum.  Its error is within a few 2^-48 of the larger product, as
+// the sloppy sum's is of its larger operand; it issues about a quarter
+// fewer instructions than two products and a sum.
+__device__ __forceinline__ ff ff_dot2(ff a, ff b, ff c, ff d) {
+  const float p = a.hi * b.hi, q = c.hi * d.hi;
+  const ff s = ff_twosum(p, q);
+  float lo = s.lo + (fmaf(a.hi, b.hi, -p) + fmaf(c.hi, d.hi, -q));
+  lo = fmaf(a.hi, b.lo, lo);
+  lo = fmaf(a.lo, b.hi, lo);
+  lo = fmaf(c.hi, d.lo, lo);
+  lo = fmaf(c.lo, d.hi, lo);
+  return ff_fast2sum(s.hi, lo);
+}
+
+// a0 b0 + a1 b1 + a2 b2 + a3 b3 the same way (a tree of three TwoSums).
+__device__ __forceinline__ ff ff_dot4(ff a0, ff b0, ff a1, ff b1, ff a2, ff b2, ff a3, ff b3) {
+  const float p0 = a0.hi * b0.hi, p1 = a1.hi * b1.hi, p2 = a2.hi * b2.hi, p3 = a3.hi * b3.hi;
+  const ff s = ff_twosum(p0, p1), t = ff_twosum(p2, p3);
+  const ff u = ff_twosum(s.hi, t.hi);
+  float lo = (fmaf(a0.hi, b0.hi, -p0) + fmaf(a1.hi, b1.hi, -p1)) +
+             (fmaf(a2.hi, b2.hi, -p2) + fmaf(a3.hi, b3.hi, -p3));
+  lo += (s.lo + t.lo) + u.lo;
+  lo = fmaf(a0.hi, b0.lo, lo);
+  lo = fmaf(a0.lo, b0.hi, lo);
+  lo = fmaf(a1.hi, b1.lo, lo);
+  lo = fmaf(a1.lo, b1.hi, lo);
+  lo = fmaf(a2.hi, b2.lo, lo);
+  lo = fmaf(a2.lo, b2.hi, lo);
+  lo = fmaf(a3.hi, b3.lo, lo);
+  lo = fmaf(a3.lo, b3.hi, lo);
+  return ff_fast2sum(u.hi, lo);
+}
+
 __device__ __forceinline__ ff ff_div(ff a, ff b) {
   const float q1 = a.hi / b.hi;
   // r = a - q1 b, exactly up to the low parts
@@ -95,17 +130,19 @@ __device__ __forceinline__ cff cff_sub(cff a, cff b) {
   return cff{ff_sub(a.re, b.re), ff_sub(a.im, b.im)};
 }
 __device__ __forceinline__ cff cff_mul(cff a, cff b) {
-  return cff{ff_sub(ff_mul(a.re, b.re), ff_mul(a.im, b.im)),
-             ff_add(ff_mul(a.re, b.im), ff_mul(a.im, b.re))};
+  return cff{ff_dot2(a.re, b.re, ff_neg(a.im), b.im), ff_dot2(a.re, b.im, a.im, b.re)};
+}
+// a x + b y of complex values, each part one four-term dot product.
+__device__ __forceinline__ cff cff_dot2(cff a, cff x, cff b, cff y) {
+  return cff{ff_dot4(a.re, x.re, ff_neg(a.im), x.im, b.re, y.re, ff_neg(b.im), y.im),
+             ff_dot4(a.re, x.im, a.im, x.re, b.re, y.im, b.im, y.re)};
 }
 __device__ __forceinline__ cff cff_conj(cff a) { return cff{a.re, ff_neg(a.im)}; }
 __device__ __forceinline__ cff cff_scale(cff a, ff s) { return cff{ff_mul(a.re, s), ff_mul(a.im, s)}; }
 __device__ __forceinline__ cff cff_scale2(cff a, float p2) {
   return cff{ff_scale2(a.re, p2), ff_scale2(a.im, p2)};
 }
-__device__ __forceinline__ ff cff_abs2(cff a) {
-  return ff_add(ff_mul(a.re, a.re), ff_mul(a.im, a.im));
-}
+__device__ __forceinline__ ff cff_abs2(cff a) { return ff_dot2(a.re, a.re, a.im, a.im); }
 __device__ __forceinline__ cff cff_div(cff a, cff b) {
   const ff inv = ff_div(ff_of(1.f), cff_abs2(b));
   return cff_scale(cff_mul(a, cff_conj(b)), inv);
@@ -128,22 +165,15 @@ struct cmff {
 };
 
 __device__ __forceinline__ cmff cmff_mul(const cmff& x, const cmff& y) {
-  return cmff{cff_add(cff_mul(x.a, y.a), cff_mul(x.b, y.c)),
-              cff_add(cff_mul(x.a, y.b), cff_mul(x.b, y.d)),
-              cff_add(cff_mul(x.c, y.a), cff_mul(x.d, y.c)),
-              cff_add(cff_mul(x.c, y.b), cff_mul(x.d, y.d))};
-}
-
-// x^2 of a complex float-float: (re^2 - im^2, 2 re im).
-__device__ __forceinline__ cff cff_sqr(cff a) {
-  return cff{ff_sub(ff_mul(a.re, a.re), ff_mul(a.im, a.im)), ff_scale2(ff_mul(a.re, a.im), 2.f)};
+  return cmff{cff_dot2(x.a, y.a, x.b, y.c), cff_dot2(x.a, y.b, x.b, y.d),
+              cff_dot2(x.c, y.a, x.d, y.c), cff_dot2(x.c, y.b, x.d, y.d)};
 }
 
 // M^2 of a 2x2 matrix: [[a^2 + bc, b (a + d)], [c (a + d), d^2 + bc]].
 __device__ __forceinline__ cmff cmff_sqr(const cmff& m) {
-  const cff bc = cff_mul(m.b, m.c), tr = cff_add(m.a, m.d);
-  return cmff{cff_add(cff_sqr(m.a), bc), cff_mul(m.b, tr), cff_mul(m.c, tr),
-              cff_add(cff_sqr(m.d), bc)};
+  const cff tr = cff_add(m.a, m.d);
+  return cmff{cff_dot2(m.a, m.a, m.b, m.c), cff_mul(m.b, tr), cff_mul(m.c, tr),
+              cff_dot2(m.d, m.d, m.b, m.c)};
 }
 
 // A column vector of two complex float-float values.
@@ -152,8 +182,7 @@ struct cvff {
 };
 
 __device__ __forceinline__ cvff cmff_apply(const cmff& m, const cvff& v) {
-  return cvff{cff_add(cff_mul(m.a, v.x), cff_mul(m.b, v.y)),
-              cff_add(cff_mul(m.c, v.x), cff_mul(m.d, v.y))};
+  return cvff{cff_dot2(m.a, v.x, m.b, v.y), cff_dot2(m.c, v.x, m.d, v.y)};
 }
 
 // Exact power-of-two rescaling so the largest component is O(1).

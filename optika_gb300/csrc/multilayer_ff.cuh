@@ -385,7 +385,7 @@ __device__ __forceinline__ cvff step_apply(const cff& q, const cff& qj, const La
                                            const cvff& v) {
   const cff a = cff_add(q, qj), b = cff_sub(q, qj);
   const cff x = cff_mul(ph.em, v.x), y = cff_mul(ph.ep, v.y);
-  return cvff{cff_add(cff_mul(a, x), cff_mul(b, y)), cff_add(cff_mul(b, x), cff_mul(a, y))};
+  return cvff{cff_dot2(a, x, b, y), cff_dot2(b, x, a, y)};
 }
 
 // First column of the step matrix of an interface alone: (q + qj, q - qj).
