@@ -8,10 +8,11 @@
 
 namespace otx {
 
-// Rays of the batch: wavelength, field angles and pupil position from two
-// Philox blocks (counter: ray index, config, block), each value formed
-// with explicitly rounded FP32 operations so that the host restatement
-// reproduces it exactly.
+// Rays of the batch: wavelength, field angles and pupil position from one
+// Philox block (counter: ray index, config, 0): four uniforms from the top
+// 24 bits of its words and a fifth from the low bytes of the first three,
+// each value formed with explicitly rounded FP32 operations so that the
+// host restatement reproduces it exactly.
 struct BatchInputs {
   float wl, fx, fy, qx, qy;
 };
@@ -19,13 +20,13 @@ struct BatchInputs {
 __device__ __forceinline__ BatchInputs batch_inputs(const otx_batch& b, int cfg, int64_t i) {
   const uint32_t k0 = (uint32_t)b.seed, k1 = (uint32_t)(b.seed >> 32);
   const u32x4 c0 = philox4x32_10(u32x4{(uint32_t)i, (uint32_t)(i >> 32), (uint32_t)cfg, 0u}, k0, k1);
-  const u32x4 c1 = philox4x32_10(u32x4{(uint32_t)i, (uint32_t)(i >> 32), (uint32_t)cfg, 1u}, k0, k1);
+  const uint32_t low = ((c0.x & 0xffu) << 24) | ((c0.y & 0xffu) << 16) | ((c0.z & 0xffu) << 8);
   BatchInputs v;
   v.wl = __fadd_rn(b.wl_lo, __fmul_rn(u01(c0.x), __fsub_rn(b.wl_hi, b.wl_lo)));
   v.fx = __fmul_rn(b.field_x_half, __fsub_rn(__fmul_rn(2.f, u01(c0.y)), 1.f));
   v.fy = __fmul_rn(b.field_y_half, __fsub_rn(__fmul_rn(2.f, u01(c0.z)), 1.f));
   v.qx = __fmul_rn(b.pupil_half, __fsub_rn(__fmul_rn(2.f, u01(c0.w)), 1.f));
-  v.qy = __fmul_rn(b.pupil_half, __fsub_rn(__fmul_rn(2.f, u01(c1.x)), 1.f));
+  v.qy = __fmul_rn(b.pupil_half, __fsub_rn(__fmul_rn(2.f, u01(low)), 1.f));
   return v;
 }
 

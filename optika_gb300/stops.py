@@ -87,6 +87,25 @@ def _api_sag_system(sag):
     return _sag_system(sag)
 
 
+def _sag_normal(lowered, x: torch.Tensor, y: torch.Tensor):
+    """Unit normals (float64 tensors) of a lowered sag at (x, y): the sag
+    kernel (otx_sag_eval, float32) with the descriptor made once."""
+    import ctypes
+
+    from . import _api
+    from . import _lib as L
+
+    n = x.numel()
+    xy = torch.stack([x.reshape(-1), y.reshape(-1)]).to(torch.float32)
+    nrm = torch.empty((3, n), dtype=torch.float32, device=x.device)
+    inp = _api._rays_struct(dict(px=xy[0], py=xy[1]), n)
+    out = _api._rays_struct(dict(dx=nrm[0], dy=nrm[1], dz=nrm[2]), n)
+    L.check(L.load().otx_sag_eval(ctypes.byref(lowered), 1, ctypes.byref(inp), ctypes.byref(out),
+                                  _api.stream_handle()), "otx_sag_eval")
+    nrm = nrm.to(torch.float64)
+    return nrm[0].reshape(x.shape), nrm[1].reshape(x.shape), nrm[2].reshape(x.shape)
+
+
 def _lower(surfaces: Sequence):
     """The descriptor of ``surfaces`` for repeated traces within one solve."""
     from . import _lib as L
@@ -97,9 +116,10 @@ def _lower(surfaces: Sequence):
 
 
 def _cached(system, key, make):
-    """A descriptor lowered once per system and key: the stop solve of a
-    system repeats for every batch of wavelengths, and the extents it gives
-    are cached on the system the same way."""
+    """A descriptor, or the wavelength-independent setup of a solve, made
+    once per system and key: the stop solve of a system repeats for every
+    batch of wavelengths, and the extents it gives are cached on the system
+    the same way."""
     cache = system.__dict__.setdefault("_stop_lowerings", {})
     if key not in cache:
         cache[key] = make()
@@ -138,7 +158,7 @@ def _trace(surfaces: Sequence, p: torch.Tensor, d: torch.Tensor, wavelength, low
     return o[:3], o[3:]
 
 
-def _newton(lowering, first, pos_f, dir_f, wl_f, tx, ty, Tl, *, free_position: bool,
+def _newton(lowering, first, pos_f, dir_f, wl_f, tx, ty, to_last: list, *, free_position: bool,
             target_direction: bool, step: float, tol: float, names: tuple) -> None:
     """The Newton iterations of every ray on the device (otx_stop_newton):
     ``pos_f`` / ``dir_f`` ([3, n] float64, system frame) are updated in
@@ -167,7 +187,7 @@ def _newton(lowering, first, pos_f, dir_f, wl_f, tx, ty, Tl, *, free_position: b
     sol.polish_steps = 2
     sol.step = float(step)
     sol.tolerance = float(tol)
-    for k, v in enumerate(Tl[:3, :4].reshape(-1).cpu().tolist()):
+    for k, v in enumerate(to_last):
         sol.to_last[k] = v
     sol.position, sol.direction, sol.wavelength = (_api.ptr(t) for t in (pos, dirn, wl))
     sol.target_x, sol.target_y, sol.status = (_api.ptr(t) for t in (txc, tyc, status))
@@ -178,6 +198,69 @@ def _newton(lowering, first, pos_f, dir_f, wl_f, tx, ty, Tl, *, free_position: b
                          f"{names[0]!r} and {names[1]!r}")
     pos_f.copy_(pos)
     dir_f.copy_(dirn)
+
+
+def _seed(sub: Sequence, samples_pupil: int, samples_field: int) -> dict:
+    """The wavelength-independent part of a stop solve between the first and
+    last surfaces of ``sub``: the boundary grids, the first guesses (aimed
+    at the first surface with power, or at the target itself), the targets
+    and the tolerances (optika/systems/_sequential.py:396-560).  Made once
+    per system and stop pair."""
+    dev = device()
+    f64 = torch.float64
+    s_first, s_last = sub[0], sub[-1]
+    gf = torch.as_tensor(s_first.aperture.wire(samples_pupil)[:, :2], dtype=f64, device=dev)
+    gl = torch.as_tensor(s_last.aperture.wire(samples_field)[:, :2], dtype=f64, device=dev)
+    shape = (gf.shape[0], gl.shape[0])
+    gx = gf[:, 0:1].expand(shape)
+    gy = gf[:, 1:2].expand(shape)
+    if not s_first.aperture.dimensionless:
+        pos = torch.stack([gx, gy, _sag(s_first.sag, gx, gy)])
+        dirn = torch.stack([torch.zeros(shape, dtype=f64, device=dev),
+                            torch.zeros(shape, dtype=f64, device=dev),
+                            torch.ones(shape, dtype=f64, device=dev)])
+        variable = "direction"
+    else:
+        dirn = torch.stack([gx, gy, torch.sqrt(1 - (gx * gx + gy * gy))])
+        pos = torch.zeros((3,) + shape, dtype=f64, device=dev)
+        variable = "position"
+
+    # seed: aim at the first surface with power, or at the target itself
+    anchor = anchor_surface(sub)
+    if anchor is s_last and not s_last.aperture.dimensionless:
+        ax_ = gl[None, :, 0].expand(shape)
+        ay_ = gl[None, :, 1].expand(shape)
+        aim = torch.stack([ax_, ay_, _sag(s_last.sag, ax_, ay_)])
+        aim = _apply(_matrix(s_last.transformation), aim)
+    else:
+        aim = _apply(_matrix(anchor.transformation),
+                     torch.zeros((3,) + shape, dtype=f64, device=dev))
+    aim = _apply(_inverse(_matrix(s_first.transformation)), aim)
+    if variable == "direction":
+        d = aim - pos
+        d = d / torch.sqrt((d * d).sum(0))
+        flip = torch.sign(d[2])
+        where = d[2] != 0
+        dirn = torch.stack([torch.where(where, flip * d[0], 0.0),
+                            torch.where(where, flip * d[1], 0.0),
+                            torch.where(where, flip * d[2], 1.0)])
+    else:
+        t = aim[2] / dirn[2]
+        px, py = aim[0] - dirn[0] * t, aim[1] - dirn[1] * t
+        pos = torch.stack([px, py, _sag(s_first.sag, px, py)])
+    M = _matrix(s_first.transformation)
+    pos = _apply(M, pos)
+    dirn = _apply(M, dirn, point=False)
+    target = "direction" if s_last.aperture.dimensionless else "position"
+    tx = gl[None, :, 0].expand(shape).reshape(-1)
+    ty = gl[None, :, 1].expand(shape).reshape(-1)
+    scale = max(float(np.ptp(gl[:, 0].cpu().numpy())), float(np.ptp(gl[:, 1].cpu().numpy())))
+    unit = max(scale, 1.0)
+    tol = max(1e-9 * unit, 4e-7 * unit)
+    dx = 1e-4 if variable == "direction" else 1e-4 * unit
+    Tl = _inverse(_matrix(s_last.transformation))
+    return dict(shape=shape, variable=variable, target=target, pos=pos, dirn=dirn, tx=tx, ty=ty,
+                tol=tol, step=dx, to_last=Tl[:3, :4].reshape(-1).cpu().tolist())
 
 
 def stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
@@ -206,60 +289,14 @@ def stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
         first_i, last_i = min(ip[0], jf[0]), max(ip[0], jf[0])
         sub = surfaces[first_i:last_i + 1]
         s_first, s_last = sub[0], sub[-1]
-        gf = torch.as_tensor(s_first.aperture.wire(samples_pupil)[:, :2], dtype=f64, device=dev)
-        gl = torch.as_tensor(s_last.aperture.wire(samples_field)[:, :2], dtype=f64, device=dev)
         if s_first.is_pupil_stop:
             ip.pop(0)
         else:
             jf.pop(0)
-        shape = (gf.shape[0], gl.shape[0])
-        gx = gf[:, 0:1].expand(shape)
-        gy = gf[:, 1:2].expand(shape)
-        if not s_first.aperture.dimensionless:
-            pos = torch.stack([gx, gy, _sag(s_first.sag, gx, gy)])
-            dirn = torch.stack([torch.zeros(shape, dtype=f64, device=dev),
-                                torch.zeros(shape, dtype=f64, device=dev),
-                                torch.ones(shape, dtype=f64, device=dev)])
-            variable = "direction"
-        else:
-            dirn = torch.stack([gx, gy, torch.sqrt(1 - (gx * gx + gy * gy))])
-            pos = torch.zeros((3,) + shape, dtype=f64, device=dev)
-            variable = "position"
-
-        # seed: aim at the first surface with power, or at the target itself
-        anchor = anchor_surface(sub)
-        if anchor is s_last and not s_last.aperture.dimensionless:
-            ax_ = gl[None, :, 0].expand(shape)
-            ay_ = gl[None, :, 1].expand(shape)
-            aim = torch.stack([ax_, ay_, _sag(s_last.sag, ax_, ay_)])
-            aim = _apply(_matrix(s_last.transformation), aim)
-        else:
-            aim = _apply(_matrix(anchor.transformation),
-                         torch.zeros((3,) + shape, dtype=f64, device=dev))
-        aim = _apply(_inverse(_matrix(s_first.transformation)), aim)
-        if variable == "direction":
-            d = aim - pos
-            d = d / torch.sqrt((d * d).sum(0))
-            flip = torch.sign(d[2])
-            where = d[2] != 0
-            dirn = torch.stack([torch.where(where, flip * d[0], 0.0),
-                                torch.where(where, flip * d[1], 0.0),
-                                torch.where(where, flip * d[2], 1.0)])
-        else:
-            t = aim[2] / dirn[2]
-            px, py = aim[0] - dirn[0] * t, aim[1] - dirn[1] * t
-            pos = torch.stack([px, py, _sag(s_first.sag, px, py)])
-        M = _matrix(s_first.transformation)
-        pos = _apply(M, pos)
-        dirn = _apply(M, dirn, point=False)
-        target = "direction" if s_last.aperture.dimensionless else "position"
-        tx = gl[None, :, 0].expand(shape).reshape(-1)
-        ty = gl[None, :, 1].expand(shape).reshape(-1)
-        scale = max(float(np.ptp(gl[:, 0].cpu().numpy())), float(np.ptp(gl[:, 1].cpu().numpy())))
-        unit = max(scale, 1.0)
-        tol = max(1e-9 * unit, 4e-7 * unit)
-        dx = 1e-4 if variable == "direction" else 1e-4 * unit
-        Tl = _inverse(_matrix(s_last.transformation))
+        plan = _cached(system, ("plan", first_i, last_i, samples_pupil, samples_field),
+                       lambda: _seed(sub, samples_pupil, samples_field))
+        shape, variable, target = plan["shape"], plan["variable"], plan["target"]
+        pos, dirn, tx, ty = plan["pos"], plan["dirn"], plan["tx"], plan["ty"]
         # every wavelength repeats the grid (wavelength-major)
         pos_f = pos.reshape(3, -1).repeat(1, nw)
         dir_f = dirn.reshape(3, -1).repeat(1, nw)
@@ -269,9 +306,9 @@ def stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
 
         lw_sub = _cached(system, ("sub", first_i, last_i), lambda: _lower(sub[1:]))
         first = _cached(system, ("sag", first_i), lambda: _api_sag_system(s_first.sag))
-        _newton(lw_sub, first, pos_f, dir_f, wl_f, tx, ty, Tl,
+        _newton(lw_sub, first, pos_f, dir_f, wl_f, tx, ty, plan["to_last"],
                 free_position=variable == "position", target_direction=target == "direction",
-                step=dx, tol=tol, names=(s_first.name, s_last.name))
+                step=plan["step"], tol=plan["tol"], names=(s_first.name, s_last.name))
         full = (3,) + ((nw,) if not scalar else ()) + shape
         out = dict(position=pos_f.reshape(full), direction=dir_f.reshape(full),
                    wavelength=wl_f.reshape(full[1:]))
@@ -296,16 +333,16 @@ def rayfunction_stops(system, wavelength, samples_pupil: int = SAMPLES_STOP,
     po, do = _trace(sub, p.reshape(3, -1), d.reshape(3, -1), st["wavelength"].reshape(-1),
                     lw_back)
     obj = sub[-1]
-    Mi = _inverse(_matrix(obj.transformation))
+    Mi = _cached(system, ("obj_inverse", min(ip, jf)), lambda: _inverse(_matrix(obj.transformation)))
     pl = _apply(Mi, po)
     dl = _apply(Mi, do, point=False)
-    from .vectors import Cartesian2dVectorArray
-
-    nrm = obj.sag.normal(Cartesian2dVectorArray(pl[0].float(), pl[1].float()))
-    dot = dl[0] * nrm.x.double() + dl[1] * nrm.y.double() + dl[2] * nrm.z.double()
+    obj_sag = _cached(system, ("object_sag", min(ip, jf)),
+                      lambda: _api_sag_system(obj.sag))
+    nx, ny, nz = _sag_normal(obj_sag, pl[0], pl[1])
+    dot = dl[0] * nx + dl[1] * ny + dl[2] * nz
     do = torch.where(dot > 0, -do, do)
     if system.transformation is not None:
-        M = _matrix(system.transformation)
+        M = _cached(system, ("system", 0), lambda: _matrix(system.transformation))
         po, do = _apply(M, po), _apply(M, do, point=False)
     ang_x = -torch.atan2(do[0], do[2])
     ang_y = -torch.asin(do[1] / torch.sqrt((do * do).sum(0)))
@@ -334,8 +371,9 @@ def extents_many(system, wavelengths) -> list[tuple]:
     if todo:
         st = rayfunction_stops(system, np.array(todo))
         f, q = st["field"], st["pupil"]
-        red = [(a.reshape(len(todo), -1).amin(1).cpu().numpy(),
-                a.reshape(len(todo), -1).amax(1).cpu().numpy()) for a in (*f, *q)]
+        g = torch.stack([a.reshape(len(todo), -1) for a in (*f, *q)])  # [4, wl, rays]
+        lo_hi = torch.stack([g.amin(2), g.amax(2)], 1).cpu().numpy()  # one read: [4, 2, wl]
+        red = [(lo_hi[i, 0], lo_hi[i, 1]) for i in range(4)]
         for j, k in enumerate(todo):
             (fx0, fx1), (fy0, fy1), (qx0, qx1), (qy0, qy1) = red
             cache[k] = ((float(fx0[j]), float(fy0[j])), (float(fx1[j]), float(fy1[j])),

@@ -43,12 +43,14 @@ def batch_inputs(seed: int, config: int, n: int, wl_lo: float, wl_hi: float, fxh
     i = np.arange(n, dtype=np.uint64)
     k0, k1 = seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF
     a = philox4x32_10(i & MASK, i >> np.uint64(32), np.uint64(config), np.uint64(0), k0, k1)
-    b = philox4x32_10(i & MASK, i >> np.uint64(32), np.uint64(config), np.uint64(1), k0, k1)
+    ff = np.uint64(0xFF)
+    low = ((a[0] & ff) << np.uint64(24)) | ((a[1] & ff) << np.uint64(16)) | (
+        (a[2] & ff) << np.uint64(8))
     f = np.float32
     two, one = f(2), f(1)
     wl = f(wl_lo) + u01(a[0]) * (f(wl_hi) - f(wl_lo))
     fx = f(fxh) * (two * u01(a[1]) - one)
     fy = f(fyh) * (two * u01(a[2]) - one)
     qx = f(pupil_half) * (two * u01(a[3]) - one)
-    qy = f(pupil_half) * (two * u01(b[0]) - one)
+    qy = f(pupil_half) * (two * u01(low) - one)
     return dict(wavelength=wl, field_x=fx, field_y=fy, pupil_x=qx, pupil_y=qy)
