@@ -493,6 +493,7 @@ def run_batched(args, rank: int, world: int, emit: bool = True) -> dict:
     bpr = 13
     pk, pk_kind = peaks()
     ach = bpr * total / (ms * 1e-3) / 1e9
+    fp32 = fp32_roofline("batched-spectrograph", total, ms, pk)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
@@ -512,12 +513,15 @@ def run_batched(args, rank: int, world: int, emit: bool = True) -> dict:
                        "schedule": {"tile": choice[0], "rays_per_thread": choice[1]},
                        "cuda_graph": True},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                         "frac": ach / pk["hbm_gbs"], "traffic": None, "peak_kind": pk_kind,
+                         "frac": ach / pk["hbm_gbs"],
+                         "traffic": _ncu_traffic("trace_batch_spectrograph_256cfg", total),
+                         "peak_kind": pk_kind,
                          "bytes_per_ray": bpr, "kernel": "k_trace_batch (spectrograph shape)",
-                         "kernel_ms": ms,
-                         "fp32": fp32_roofline("batched-spectrograph", total, ms, pk),
-                         "note": "compute-bound (FP32 issue): the byte roofline is shown for "
-                                 "completeness"},
+                         "kernel_ms": ms, "fp32": fp32, "issue": issue_roofline(
+                             "trace_batch_spectrograph_256cfg", total, ms, pk, fp32),
+                         "note": "compute-bound (instruction issue): the byte roofline is "
+                                 "shown for completeness; traffic scaled from the 256-"
+                                 "configuration capture by rays"},
             "cpu_baseline": cpu, "gpu_launches": 3, "clocks": clk,
     }
     if emit and rank == 0:
@@ -827,8 +831,8 @@ def run_stops(args, rank: int, world: int) -> None:
     cpu = None
     if rank == 0 and not args.no_cpu:
         cores = len(os.sched_getaffinity(0))
-        # 4 jobs of 64 wavelengths per core (each a float64 solve)
-        edges = np.linspace(500.0, 600.0, 4 * cores + 1)
+        # 16 jobs of 64 wavelengths per core (each a float64 solve)
+        edges = np.linspace(500.0, 600.0, 16 * cores + 1)
         jobs = [(float(a), float(b), 64) for a, b in zip(edges[:-1], edges[1:])]
         solves, wall = _cpu_pool(_cpu_stops_worker, jobs, cores)
         cpu = {"value": solves / wall, "unit": "solves/s", "cores": cores, "kind": "port",

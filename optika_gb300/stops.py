@@ -159,13 +159,15 @@ def _trace(surfaces: Sequence, p: torch.Tensor, d: torch.Tensor, wavelength, low
 
 
 def _newton(lowering, first, pos_f, dir_f, wl_f, tx, ty, to_last: list, *, free_position: bool,
-            target_direction: bool, step: float, tol: float, names: tuple) -> None:
+            target_direction: bool, step: float, tol: float) -> torch.Tensor:
     """The Newton iterations of every ray on the device (otx_stop_newton):
     ``pos_f`` / ``dir_f`` ([3, n] float64, system frame) are updated in
     place with the solved rays.  One thread per ray: each iteration traces
     the ray and its two finite-difference perturbations and applies the
     2 x 2 update; a ray whose residual drops below ``tol`` takes two more
-    steps.  The host reads only the per-ray status at the end."""
+    steps.  Returns a device flag, true when some ray did not converge:
+    the host reads it with the results, so nothing waits for the solve
+    before the work that follows it is queued."""
     import ctypes
 
     from . import _api
@@ -193,11 +195,9 @@ def _newton(lowering, first, pos_f, dir_f, wl_f, tx, ty, to_last: list, *, free_
     sol.target_x, sol.target_y, sol.status = (_api.ptr(t) for t in (txc, tyc, status))
     L.check(L.load().otx_stop_newton(ctypes.byref(lowering.sys), ctypes.byref(first),
                                      ctypes.byref(sol), _api.stream_handle()), "otx_stop_newton")
-    if bool((status < 0).any()):
-        raise ValueError(f"could not solve for the rays connecting the stop surfaces "
-                         f"{names[0]!r} and {names[1]!r}")
     pos_f.copy_(pos)
     dir_f.copy_(dirn)
+    return (status < 0).any()
 
 
 def _seed(sub: Sequence, samples_pupil: int, samples_field: int) -> dict:
@@ -271,7 +271,16 @@ def stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
     array: every wavelength is solved in the same Newton iterations (one
     trace launch per iteration for all of them) and the arrays gain a
     wavelength axis after the first, [3, wavelength, first wire, last
-    wire]."""
+    wire].  Raises ValueError when some ray does not converge."""
+    out = _stops_only(system, wavelength, samples_pupil, samples_field)
+    _check([bool(f) for f in out.pop("failed")], out.pop("stops"))
+    return out
+
+
+def _stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
+                samples_field: int = SAMPLES_STOP) -> dict:
+    """:func:`stops_only` without reading the convergence flags: ``failed``
+    holds one device flag per stop pair and ``stops`` their names."""
     scalar = np.ndim(wavelength) == 0
     wls = np.atleast_1d(np.asarray(wavelength, dtype=np.float64))
     nw = len(wls)
@@ -285,6 +294,7 @@ def stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
     dev = device()
     f64 = torch.float64
     out = None
+    flags, names = [], []
     while ip and jf:
         first_i, last_i = min(ip[0], jf[0]), max(ip[0], jf[0])
         sub = surfaces[first_i:last_i + 1]
@@ -306,13 +316,25 @@ def stops_only(system, wavelength, samples_pupil: int = SAMPLES_STOP,
 
         lw_sub = _cached(system, ("sub", first_i, last_i), lambda: _lower(sub[1:]))
         first = _cached(system, ("sag", first_i), lambda: _api_sag_system(s_first.sag))
-        _newton(lw_sub, first, pos_f, dir_f, wl_f, tx, ty, plan["to_last"],
-                free_position=variable == "position", target_direction=target == "direction",
-                step=plan["step"], tol=plan["tol"], names=(s_first.name, s_last.name))
+        failed = _newton(lw_sub, first, pos_f, dir_f, wl_f, tx, ty, plan["to_last"],
+                         free_position=variable == "position",
+                         target_direction=target == "direction", step=plan["step"],
+                         tol=plan["tol"])
+        flags.append(failed)
+        names.append((s_first.name, s_last.name))
         full = (3,) + ((nw,) if not scalar else ()) + shape
         out = dict(position=pos_f.reshape(full), direction=dir_f.reshape(full),
                    wavelength=wl_f.reshape(full[1:]))
+    out.update(failed=flags, stops=names)
     return out
+
+
+def _check(failed: list, stops: list) -> None:
+    """Raise for the first stop pair whose solve did not converge."""
+    for f, (a, b) in zip(failed, stops):
+        if f:
+            raise ValueError(f"could not solve for the rays connecting the stop surfaces "
+                             f"{a!r} and {b!r}")
 
 
 def rayfunction_stops(system, wavelength, samples_pupil: int = SAMPLES_STOP,
@@ -321,8 +343,18 @@ def rayfunction_stops(system, wavelength, samples_pupil: int = SAMPLES_STOP,
     into the system, with the field and pupil grids they give: angles
     (rad) for the side at infinity, positions (mm) for the other
     (optika/systems/_sequential.py:695-754).  A 1-D ``wavelength`` adds a
-    leading wavelength axis to every grid."""
-    st = stops_only(system, wavelength, samples_pupil, samples_field)
+    leading wavelength axis to every grid.  Raises ValueError when some
+    ray of the stop solve does not converge."""
+    out = _rayfunction_stops(system, wavelength, samples_pupil, samples_field)
+    _check([bool(f) for f in out.pop("failed")], out.pop("stops"))
+    return out
+
+
+def _rayfunction_stops(system, wavelength, samples_pupil: int = SAMPLES_STOP,
+                       samples_field: int = SAMPLES_STOP) -> dict:
+    """:func:`rayfunction_stops` with the convergence flags left on the
+    device (``failed``, ``stops`` as in :func:`_stops_only`)."""
+    st = _stops_only(system, wavelength, samples_pupil, samples_field)
     surfaces = system.surfaces_all
     ip = max(i for i, s in enumerate(surfaces) if s.is_pupil_stop)
     jf = max(i for i, s in enumerate(surfaces) if s.is_field_stop)
@@ -352,7 +384,8 @@ def rayfunction_stops(system, wavelength, samples_pupil: int = SAMPLES_STOP,
         field, pupil = (po[0], po[1]), (ang_x, ang_y)
     return dict(position=po.reshape((3,) + shape), direction=do.reshape((3,) + shape),
                 field=tuple(f.reshape(shape) for f in field),
-                pupil=tuple(q.reshape(shape) for q in pupil))
+                pupil=tuple(q.reshape(shape) for q in pupil), failed=st["failed"],
+                stops=st["stops"])
 
 
 def extents(system, wavelength: float) -> tuple:
@@ -369,10 +402,14 @@ def extents_many(system, wavelengths) -> list[tuple]:
     keys = [float(w) for w in np.atleast_1d(np.asarray(wavelengths, dtype=np.float64))]
     todo = sorted({k for k in keys if k not in cache})
     if todo:
-        st = rayfunction_stops(system, np.array(todo))
+        st = _rayfunction_stops(system, np.array(todo))
         f, q = st["field"], st["pupil"]
         g = torch.stack([a.reshape(len(todo), -1) for a in (*f, *q)])  # [4, wl, rays]
-        lo_hi = torch.stack([g.amin(2), g.amax(2)], 1).cpu().numpy()  # one read: [4, 2, wl]
+        lo_hi = torch.stack([g.amin(2), g.amax(2)], 1).reshape(-1)
+        flags = torch.stack(st["failed"]).to(lo_hi.dtype)
+        host = torch.cat([lo_hi, flags]).cpu().numpy()  # the one read of the solve
+        _check(list(host[lo_hi.numel():] != 0), st["stops"])
+        lo_hi = host[:lo_hi.numel()].reshape(4, 2, len(todo))
         red = [(lo_hi[i, 0], lo_hi[i, 1]) for i in range(4)]
         for j, k in enumerate(todo):
             (fx0, fx1), (fy0, fy1), (qx0, qx1), (qy0, qy1) = red

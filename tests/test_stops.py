@@ -136,3 +136,21 @@ def test_gpu_normalized_raytrace(cuda):
     assert np.abs(oa["py"][m] - ob["py"][m]).max() < 1e-4
     # the pupil corners reach the stop's edge: some rays are vignetted, not all
     assert 0 < m.sum() < m.size
+
+
+@pytest.mark.gpu
+def test_gpu_stop_solve_reports_rays_that_do_not_converge(cuda, monkeypatch):
+    """A solve whose rays stop short of the tolerance (here: one Newton
+    iteration allowed) raises, through the public calls and through the
+    batched extents, whose single read of the results carries the flag."""
+    from optika_gb300 import stops
+
+    monkeypatch.setattr(stops, "MAX_ITER", 1)
+    for call in (lambda s: stops.rayfunction_stops(s, 500.0),
+                 lambda s: stops.stops_only(s, 500.0),
+                 lambda s: stops.extents_many(s, [500.0, 550.0])):
+        with pytest.raises(ValueError, match="could not solve"):
+            call(configs.stop_grazing())
+    # the full iteration count solves the same system
+    monkeypatch.setattr(stops, "MAX_ITER", 60)
+    assert len(stops.extents_many(configs.stop_grazing(), [500.0, 550.0])) == 2
