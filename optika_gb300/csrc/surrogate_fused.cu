@@ -6,16 +6,25 @@
 // batched trace does), pack the 9 network inputs as BF16 straight into
 // shared memory in the 128-byte-swizzled K-major layout the tensor cores
 // read, and keep the quadratic baseline of the image position in
-// registers.  One thread issues every tcgen05.mma (M = 128, N = 256, FP32
+// registers.  One thread issues every tcgen05.mma (M = 128, FP32
 // accumulators in TMEM, 256 columns per tile); another streams the weight
 // matrices from L2 by TMA through a ring of 32 KB stages (the output
 // layer's weights stay resident).  Each weight stage feeds both tiles'
-// MMAs, so a weight byte fetched from L2 serves 256 rays.  After each layer
-// the tiles' epilogue warps read the accumulators with tcgen05.ld, add the
-// bias, apply SiLU (packed BF16 tanh and FMA, one MUFU operation per two
-// values) and write the next layer's BF16 input back into the tile's
-// shared-memory operand.  Activations never
-// leave the SM.  After the output layer a
+// MMAs, so a weight byte fetched from L2 serves 256 rays.
+//
+// A hidden layer runs in column halves (N = 128 per MMA) and its weights in
+// (column half, K half) stages, in the order (0-127, K 0-127),
+// (0-127, K 128-255), (128-255, K 0-127), (128-255, K 128-255).  Four of a
+// tile's epilogue warps own accumulator columns 0-127 and the other four
+// columns 128-255; each group reads its half with tcgen05.ld, adds the
+// bias, applies SiLU (packed BF16 tanh and FMA) and writes the next layer's
+// BF16 input of the same K columns back into the tile's operand.  The
+// first group starts once the third stage's MMAs have completed (the last
+// ones to read K columns 0-127), so its epilogue overlaps the fourth
+// stage's MMAs, and the second group's epilogue overlaps the next layer's
+// first stage: the tensor cores and the epilogue warps work at the same
+// time instead of in turn.  Activations never leave the SM.  After the
+// output layer a
 // ray of a trusted configuration whose vignetting logit is at least the
 // band away from 0 lands at baseline + out_scale * network output (binned
 // into its configuration's image if the logit is positive); every other
@@ -43,8 +52,9 @@ constexpr int F_WIDTH = 256;                         // hidden width
 constexpr int F_KC = 64;                             // K elements per 128-byte chunk
 constexpr int F_A_CHUNK = F_ROWS * F_KC * 2;         // 16 KB: one K chunk of a tile
 constexpr int F_A_BYTES = (F_WIDTH / F_KC) * F_A_CHUNK;  // 64 KB: a tile's operand
-constexpr int F_NH = 256;                            // weight rows (N) per stage
-constexpr int F_STAGE = F_NH * F_KC * 2;             // 32 KB
+constexpr int F_NH = 128;                            // weight rows (N) per stage: a column half
+constexpr int F_WBOX = F_NH * F_KC * 2;              // 16 KB: one TMA box, one K chunk
+constexpr int F_STAGE = 2 * F_WBOX;                  // 32 KB: a K half (two chunks)
 constexpr int F_STAGES = 2;
 constexpr int F_OUT_N = 16;                          // output layer N (3 used)
 constexpr int F_WOUT_CHUNK = F_OUT_N * F_KC * 2;     // 2 KB
@@ -117,9 +127,11 @@ __global__ void __launch_bounds__(F_THREADS, 1)
   float* bout = hb + F_MAX_HIDDEN * F_WIDTH;
   uint64_t* wfull = reinterpret_cast<uint64_t*>(bout + F_OUT_N);
   uint64_t* wempty = wfull + F_STAGES;
-  uint64_t* afull = wempty + F_STAGES;   // [2]
-  uint64_t* accfull = afull + 2;         // [2]
-  uint64_t* woutfull = accfull + 2;
+  uint64_t* lo_ready = wempty + F_STAGES;  // [2] K columns 0-127 of a tile's operand written
+  uint64_t* hi_ready = lo_ready + 2;       // [2] K columns 128-255 written
+  uint64_t* acc0_full = hi_ready + 2;      // [2] accumulator columns 0-127 complete
+  uint64_t* acc1_full = acc0_full + 2;     // [2] accumulator columns 128-255 complete
+  uint64_t* woutfull = acc1_full + 2;
   uint64_t* mmadone = woutfull + 1;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(mmadone + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);
@@ -136,8 +148,10 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       mbar_init(&wempty[s], 1);
     }
     for (int g = 0; g < 2; ++g) {
-      mbar_init(&afull[g], 32 * F_EPI_WARPS);
-      mbar_init(&accfull[g], 1);
+      mbar_init(&lo_ready[g], 32 * F_EPI_WARPS / 2);
+      mbar_init(&hi_ready[g], 32 * F_EPI_WARPS / 2);
+      mbar_init(&acc0_full[g], 1);
+      mbar_init(&acc1_full[g], 1);
     }
     mbar_init(woutfull, 1);
     mbar_init(mmadone, 1);
@@ -158,10 +172,13 @@ __global__ void __launch_bounds__(F_THREADS, 1)
       for (int kc = 0; kc < F_WIDTH / F_KC; ++kc)
         tma_load_2d(swo + kc * F_WOUT_CHUNK, &maps.out, kc * F_KC, 0, woutfull);
       bool ok = true;
+      // stages in the issuer's order: layer 0 as two column halves (one
+      // K chunk each, K = 16 used); every hidden layer as (columns 0-127,
+      // K 0-127), (0-127, 128-255), (128-255, 0-127), (128-255, 128-255)
       for (int64_t p = blockIdx.x; ok && p < a.num_pairs; p += gridDim.x) {
         for (int l = 0; ok && l < L; ++l) {
-          const int nk = l == 0 ? 1 : F_WIDTH / F_KC;
-          for (int kc = 0; kc < nk; ++kc) {
+          const int ns = l == 0 ? 2 : 4;
+          for (int j = 0; j < ns; ++j) {
             const int s = (int)(k % F_STAGES);
             if (k >= F_STAGES &&
                 (aborted(abort_flag) ||
@@ -169,8 +186,16 @@ __global__ void __launch_bounds__(F_THREADS, 1)
               ok = false;
               break;
             }
-            mbar_expect_tx(&wfull[s], F_STAGE);
-            tma_load_2d(sw + s * F_STAGE, &maps.w[l], kc * F_KC, 0, &wfull[s]);
+            uint8_t* dst = sw + s * F_STAGE;
+            if (l == 0) {
+              mbar_expect_tx(&wfull[s], F_WBOX);
+              tma_load_2d(dst, &maps.w[0], 0, j * F_NH, &wfull[s]);
+            } else {
+              const int h = j >> 1, kh = j & 1;
+              mbar_expect_tx(&wfull[s], F_STAGE);
+              tma_load_2d(dst, &maps.w[l], kh * 2 * F_KC, h * F_NH, &wfull[s]);
+              tma_load_2d(dst + F_WBOX, &maps.w[l], kh * 2 * F_KC + F_KC, h * F_NH, &wfull[s]);
+            }
             ++k;
           }
         }
@@ -189,57 +214,91 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     if (lane == 0) {
       constexpr uint32_t ID_H = idesc_bf16(F_ROWS, F_NH);
       constexpr uint32_t ID_O = idesc_bf16(F_ROWS, F_OUT_N);
-      int64_t k = 0;
-      uint32_t ap[2] = {0u, 0u};
+      int64_t k = 0;                          // weight stages consumed
+      uint32_t lp[2] = {0u, 0u}, hp[2] = {0u, 0u};  // lo_ready / hi_ready parities
       bool ok = mbar_wait(woutfull, 0);
-      for (int64_t p = blockIdx.x; ok && p < a.num_pairs; p += gridDim.x) {
-        for (int l = 0; ok && l <= L; ++l) {
-          // both tiles' inputs of this layer are in shared memory
-          for (int g = 0; ok && g < 2; ++g) {
-            if (aborted(abort_flag) || !mbar_wait(&afull[g], ap[g])) {
-              ok = false;
-              break;
-            }
-            ap[g] ^= 1u;
+      // wait for both tiles' operand half (lo_ready or hi_ready)
+      auto wait_half = [&](uint64_t* bars, uint32_t* par) {
+        for (int g = 0; ok && g < 2; ++g) {
+          if (aborted(abort_flag) || !mbar_wait(&bars[g], par[g])) {
+            ok = false;
+            break;
           }
-          if (!ok) break;
-          tc_fence_after();
-          if (l < L) {
-            const int nk = l == 0 ? 1 : F_WIDTH / F_KC;
-            const int nkk = l == 0 ? 1 : F_KC / 16;  // layer 0: K = 16 (9 inputs, zero padded)
-            for (int kc = 0; kc < nk; ++kc) {
-              const int s = (int)(k % F_STAGES);
-              if (!mbar_wait(&wfull[s], (uint32_t)((k / F_STAGES) & 1))) {
-                ok = false;
-                break;
-              }
-              tc_fence_after();
-              const uint64_t bd = desc_sw128(sw + s * F_STAGE);
-              for (int g = 0; g < 2; ++g) {
-                const uint64_t ad = desc_sw128(sa + g * F_A_BYTES + kc * F_A_CHUNK);
-                const uint32_t acc = tbase + (uint32_t)(g * F_WIDTH);
-                for (int kk = 0; kk < nkk; ++kk)
-                  umma_bf16(acc, ad + 2 * kk, bd + 2 * kk, ID_H, (kc | kk) != 0);
-              }
-              umma_commit(&wempty[s]);
-              ++k;
-            }
-          } else {
-            for (int g = 0; g < 2; ++g) {
-              const uint32_t acc = tbase + (uint32_t)(g * F_WIDTH);
-              for (int kc = 0; kc < F_WIDTH / F_KC; ++kc) {
-                const uint64_t ad = desc_sw128(sa + g * F_A_BYTES + kc * F_A_CHUNK);
-                const uint64_t bd = desc_sw128(swo + kc * F_WOUT_CHUNK);
-                for (int kk = 0; kk < F_KC / 16; ++kk)
-                  umma_bf16(acc, ad + 2 * kk, bd + 2 * kk, ID_O, (kc | kk) != 0);
-              }
-            }
-          }
-          if (ok) {
-            umma_commit(&accfull[0]);
-            umma_commit(&accfull[1]);
+          par[g] ^= 1u;
+        }
+        if (ok) tc_fence_after();
+      };
+      // one weight stage into column half h of both tiles' accumulators:
+      // K chunks kc0, kc0 + 1 of the operand (nkk MMAs of K = 16 each);
+      // accumulate unless `fresh` and first
+      auto stage = [&](int h, int kc0, int nchunks, int nkk, bool fresh) {
+        const int s = (int)(k % F_STAGES);
+        if (!ok || !mbar_wait(&wfull[s], (uint32_t)((k / F_STAGES) & 1))) {
+          ok = false;
+          return;
+        }
+        tc_fence_after();
+        for (int g = 0; g < 2; ++g) {
+          const uint32_t acc = tbase + (uint32_t)(g * F_WIDTH + h * F_NH);
+          for (int c = 0; c < nchunks; ++c) {
+            const uint64_t ad = desc_sw128(sa + g * F_A_BYTES + (kc0 + c) * F_A_CHUNK);
+            const uint64_t bd = desc_sw128(sw + s * F_STAGE + c * F_WBOX);
+            for (int kk = 0; kk < nkk; ++kk)
+              umma_bf16(acc, ad + 2 * kk, bd + 2 * kk, ID_H, !(fresh && c == 0 && kk == 0));
           }
         }
+        umma_commit(&wempty[s]);
+        ++k;
+      };
+      // Each hidden layer runs in column halves so that a half's epilogue
+      // overlaps the other half's MMAs: the epilogue of columns 0-127
+      // (which writes the next layer's K columns 0-127 over this layer's)
+      // starts once every MMA reading K columns 0-127 has completed, while
+      // the MMAs of columns 128-255 over K 128-255 still run.
+      for (int64_t p = blockIdx.x; ok && p < a.num_pairs; p += gridDim.x) {
+        for (int l = 0; ok && l < L; ++l) {
+          if (l == 0) {
+            wait_half(lo_ready, lp);  // ray inputs (K = 16, zero padded)
+            stage(0, 0, 1, 1, true);
+            stage(1, 0, 1, 1, true);
+            if (ok) {
+              umma_commit(&acc0_full[0]);
+              umma_commit(&acc0_full[1]);
+              umma_commit(&acc1_full[0]);
+              umma_commit(&acc1_full[1]);
+            }
+            continue;
+          }
+          wait_half(lo_ready, lp);  // epilogue of columns 0-127 of layer l - 1 done
+          stage(0, 0, 2, F_KC / 16, true);
+          wait_half(hi_ready, hp);  // epilogue of columns 128-255 done
+          stage(0, 2, 2, F_KC / 16, false);
+          stage(1, 0, 2, F_KC / 16, true);
+          if (ok) {  // columns 0-127 complete; K 0-127 of the operand read
+            umma_commit(&acc0_full[0]);
+            umma_commit(&acc0_full[1]);
+          }
+          stage(1, 2, 2, F_KC / 16, false);
+          if (ok) {
+            umma_commit(&acc1_full[0]);
+            umma_commit(&acc1_full[1]);
+          }
+        }
+        // output layer: resident weights, N = 16, into columns 0-15
+        wait_half(lo_ready, lp);
+        wait_half(hi_ready, hp);
+        if (!ok) break;
+        for (int g = 0; g < 2; ++g) {
+          const uint32_t acc = tbase + (uint32_t)(g * F_WIDTH);
+          for (int kc = 0; kc < F_WIDTH / F_KC; ++kc) {
+            const uint64_t ad = desc_sw128(sa + g * F_A_BYTES + kc * F_A_CHUNK);
+            const uint64_t bd = desc_sw128(swo + kc * F_WOUT_CHUNK);
+            for (int kk = 0; kk < F_KC / 16; ++kk)
+              umma_bf16(acc, ad + 2 * kk, bd + 2 * kk, ID_O, (kc | kk) != 0);
+          }
+        }
+        umma_commit(&acc0_full[0]);
+        umma_commit(&acc0_full[1]);
       }
       if (!ok) {
         *abort_flag = 1;
@@ -263,7 +322,11 @@ __global__ void __launch_bounds__(F_THREADS, 1)
     const float* coef = reinterpret_cast<const float*>(a.sg.baseline);
     const uint8_t* trusted = reinterpret_cast<const uint8_t*>(a.sg.trusted);
     const bool bin = a.img.counts || a.img.flux;
-    uint32_t cp = 0u;  // accfull parity
+    // this warp's column half: its accumulator barrier and the operand half
+    // it writes (columns 0-127 also take the ray inputs and the output layer)
+    uint64_t* my_full = ch == 0 ? &acc0_full[g] : &acc1_full[g];
+    uint64_t* my_ready = ch == 0 ? &lo_ready[g] : &hi_ready[g];
+    uint32_t cp = 0u;  // my_full parity
     unsigned long long n_rays = 0, n_net = 0, n_fb = 0;
     bool ok = true;
     for (int64_t p = blockIdx.x; ok && p < a.num_pairs; p += gridDim.x) {
@@ -294,13 +357,15 @@ __global__ void __launch_bounds__(F_THREADS, 1)
         const int sx = row & 7;
         *reinterpret_cast<uint4*>(rp + ((0 ^ sx) << 4)) = make_uint4(w[0], w[1], w[2], w[3]);
         *reinterpret_cast<uint4*>(rp + ((1 ^ sx) << 4)) = make_uint4(w[4], w[5], w[6], w[7]);
+        fence_proxy_async_smem();
+        tc_fence_before();
+        mbar_arrive(my_ready);
       }
-      fence_proxy_async_smem();
-      tc_fence_before();
-      mbar_arrive(&afull[g]);
-      // ---- hidden layers: TMEM -> bias, SiLU -> BF16 operand of the next layer
+      // ---- hidden layers: TMEM -> bias, SiLU -> BF16 operand of the next
+      // layer, this warp's column half (the next layer's K columns of the
+      // same numbers)
       for (int l = 0; l < L; ++l) {
-        if (aborted(abort_flag) || !mbar_wait(&accfull[g], cp)) {
+        if (aborted(abort_flag) || !mbar_wait(my_full, cp)) {
           ok = false;
           break;
         }
@@ -325,17 +390,18 @@ __global__ void __launch_bounds__(F_THREADS, 1)
         epilogue_block(rb, hbl, A, ch * 128 + 96, row);
         fence_proxy_async_smem();
         tc_fence_before();
-        mbar_arrive(&afull[g]);
+        mbar_arrive(my_ready);
       }
       if (!ok) break;
+      if (ch != 0) continue;
       // ---- output layer: land, bin or queue for the trace
-      if (aborted(abort_flag) || !mbar_wait(&accfull[g], cp)) {
+      if (aborted(abort_flag) || !mbar_wait(my_full, cp)) {
         ok = false;
         break;
       }
       cp ^= 1u;
       tc_fence_after();
-      if (ch == 0) {
+      {
         float v[16];
         __syncwarp();
         tmem_ld16(tacc, v);
