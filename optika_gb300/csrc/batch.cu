@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const __grid_constant__ otx
   const bool bin = image_any(a.img);
   int bin_skip = 0;
   int cur = -1;
+  bool skip0 = false;
   for (;;) {
     __syncthreads();  // previous item done: s_item and surf may be rewritten
     if (tid == 0) s_item = (int)atomicAdd(counter, 1u);
@@ -63,6 +64,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const __grid_constant__ otx
       }
       __syncthreads();
       cur = cfg;
+      skip0 = batch_first_is_noop(surf[0]);
     }
     const int64_t base = offs[cfg];
     const int64_t n_c = offs[cfg + 1] - base;
@@ -74,7 +76,7 @@ __global__ void __launch_bounds__(256) k_trace_batch(const __grid_constant__ otx
         const int64_t i = i0 + (int64_t)k * blockDim.x;
         if (i < end) {
           batch_ray(b, cfg, i, r[k]);
-          propagate_all<Ks...>(sys, surf, r[k]);
+          propagate_all<Ks...>(sys, surf, r[k], skip0);
         }
       }
 #pragma unroll

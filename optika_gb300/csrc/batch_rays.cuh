@@ -53,13 +53,36 @@ __device__ __forceinline__ void propagate_smem(const otx_system& sys, const otx_
   if constexpr (sizeof...(Rest) > 0) propagate_smem<I + 1, Rest...>(sys, s, r);
 }
 
+// Whether the first surface leaves a batch ray unchanged: batch rays start
+// on the z = 0 plane of the input frame in vacuum (n = 1, no attenuation),
+// so a flat vacuum surface without aperture or rulings in that frame has its
+// intercept at t = 0 and keeps the direction (the condition of
+// first_is_noop, read from the staged descriptor).
+__device__ __forceinline__ bool batch_first_is_noop(const otx_surface& s) {
+  const otx_affine& f = s.to_local;
+  return s.sag_type == OTX_SAG_FLAT && s.mat_type == OTX_MAT_VACUUM &&
+         s.aper_type == OTX_APER_NONE && s.rule_type == OTX_RULE_NONE &&
+         (f.flags & OTX_AFFINE_ROT_IDENTITY) && f.t_hi[0] == 0.f && f.t_hi[1] == 0.f &&
+         f.t_hi[2] == 0.f && f.t_lo[0] == 0.f && f.t_lo[1] == 0.f && f.t_lo[2] == 0.f;
+}
+
+template <class K0, class... Rest>
+__device__ __forceinline__ void propagate_smem_skip(const otx_system& sys, const otx_surface* s,
+                                                    Ray& r, bool skip0) {
+  if (!skip0) propagate_surface<K0, false>(sys, s[0], r);
+  if constexpr (sizeof...(Rest) > 0) propagate_smem<1, Rest...>(sys, s, r);
+}
+
+// All surfaces of the staged sequence; skip0 (batch_first_is_noop of the
+// first) leaves out the first step.
 template <class... Ks>
 __device__ __forceinline__ void propagate_all(const otx_system& sys, const otx_surface* s,
-                                              Ray& r) {
+                                              Ray& r, bool skip0 = false) {
   if constexpr (sizeof...(Ks) > 0) {
-    propagate_smem<0, Ks...>(sys, s, r);
+    propagate_smem_skip<Ks...>(sys, s, r, skip0);
   } else {
-    for (int k = 0; k < sys.num_surfaces; ++k) propagate_surface<AnyKind, true>(sys, s[k], r);
+    for (int k = skip0 ? 1 : 0; k < sys.num_surfaces; ++k)
+      propagate_surface<AnyKind, true>(sys, s[k], r);
   }
 }
 

@@ -523,4 +523,48 @@ __device__ __forceinline__ void periodic_bilayer_ff(const otx_periodic_stack& P,
   Tp = T[1];
 }
 
+// R and T of one polarisation of a periodic bilayer mirror, two lanes per
+// sample: the even lane of a lane pair takes s, the odd lane p.  The even
+// lane evaluates layer A's medium factor and phase, the odd lane layer B's,
+// and the pair exchanges them by shuffles (both lanes of a pair always run
+// together); each lane then forms its own polarisation's product.  Half the
+// state of periodic_bilayer_ff per thread, twice the threads.
+__device__ __forceinline__ void periodic_bilayer_lane_ff(const otx_periodic_stack& P, float wl,
+                                                         float cos0, cf n0, float& R, float& T) {
+  const int lane = threadIdx.x & 31;
+  const bool odd = lane & 1;
+  const unsigned pair = 3u << (lane & ~1);
+  const cff n0c = cff_of(n0.re, n0.im);
+  const ff one_m_c2 = ff_sub(ff_of(1.f), ff_mul(ff_of(cos0), ff_of(cos0)));
+  const cff inv0 = cff_scale(cff_mul(n0c, n0c), one_m_c2);
+  const cf na{P.n_a_re, P.n_a_im}, nb{P.n_b_re, P.n_b_im}, ns{P.n_sub_re, P.n_sub_im};
+  // this lane's layer: A on even lanes, B on odd lanes
+  const cf nl = odd ? nb : na;
+  const cff wl_mine = medium_w_ff(inv0, nl);
+  const LayerPhase ph = layer_phase_ff(wl_mine, odd ? P.thickness_b : P.thickness_a, wl);
+  const cff ws = medium_w_ff(inv0, ns);
+  auto xch = [&](float v) { return __shfl_xor_sync(pair, v, 1); };
+  const cff w_other{{xch(wl_mine.re.hi), xch(wl_mine.re.lo)}, {xch(wl_mine.im.hi), xch(wl_mine.im.lo)}};
+  LayerPhase po;
+  po.em = cff{{xch(ph.em.re.hi), xch(ph.em.re.lo)}, {xch(ph.em.im.hi), xch(ph.em.im.lo)}};
+  po.ep = cff{{xch(ph.ep.re.hi), xch(ph.ep.re.lo)}, {xch(ph.ep.im.hi), xch(ph.ep.im.lo)}};
+  po.prop = __shfl_xor_sync(pair, (int)ph.prop, 1) != 0;
+  const cff wa = odd ? w_other : wl_mine, wb = odd ? wl_mine : w_other;
+  const LayerPhase& A = odd ? po : ph;
+  const LayerPhase& B = odd ? ph : po;
+  cff q0, qa, qb, qs;
+  if (!odd) {
+    q0 = cff_scale(n0c, ff_of(cos0));
+    qa = wa;
+    qb = wb;
+    qs = ws;
+  } else {
+    q0 = cff_scale(cff_conj(n0c), ff_div(ff_of(cos0), cff_abs2(n0c)));
+    qa = p_factor(wa, na);
+    qb = p_factor(wb, nb);
+    qs = p_factor(ws, ns);
+  }
+  bilayer_pol_ff(q0, qa, qb, qs, A, B, P.num_periods, R, T);
+}
+
 }  // namespace otx
