@@ -121,6 +121,7 @@ def _cached(system, key, make):
     batch of wavelengths, and the extents it gives are cached on the system
     the same way."""
     cache = system.__dict__.setdefault("_stop_lowerings", {})
+    key = (str(device()),) + tuple(key)  # descriptors and tensors live on one device
     if key not in cache:
         cache[key] = make()
     return cache[key]
