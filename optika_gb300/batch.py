@@ -153,7 +153,8 @@ class BatchedTrace:
     def config_slice(self, c: int) -> slice:
         return slice(int(self.ray_offset_host[c]), int(self.ray_offset_host[c + 1]))
 
-    def tune(self, candidates=((2048, 1), (8192, 1), (32768, 1), (8192, 2), (32768, 2)),
+    def tune(self, candidates=((512, 1), (1024, 1), (2048, 1), (8192, 1), (32768, 1), (8192, 2),
+                               (32768, 2)),
              repeats: int = 3) -> tuple:
         """Time each (tile size, rays per thread) and keep the fastest; the
         choice is cached per shape, configuration count and ray total."""
