@@ -483,52 +483,12 @@ __device__ __forceinline__ cff p_factor(const cff& w, cf nj_f) {
   return cff_scale(cff_conj(w), ff_div(ff_of(1.f), cff_abs2(cff_of(nj_f.re, nj_f.im))));
 }
 
-// R and T, s and p, of a periodic bilayer mirror (float-float): the layer
-// phases are evaluated once per sample.
-__device__ __forceinline__ void periodic_bilayer_ff(const otx_periodic_stack& P, float wl,
-                                                    float cos0, cf n0, float& Rs, float& Rp,
-                                                    float& Ts, float& Tp) {
-  const cff n0c = cff_of(n0.re, n0.im);
-  const ff one_m_c2 = ff_sub(ff_of(1.f), ff_mul(ff_of(cos0), ff_of(cos0)));
-  const cff inv0 = cff_scale(cff_mul(n0c, n0c), one_m_c2);
-  const cf na{P.n_a_re, P.n_a_im}, nb{P.n_b_re, P.n_b_im}, ns{P.n_sub_re, P.n_sub_im};
-  const cff wa = medium_w_ff(inv0, na), wb = medium_w_ff(inv0, nb), ws = medium_w_ff(inv0, ns);
-  LayerPhase ph[2];
-#pragma unroll 1
-  for (int j = 0; j < 2; ++j)
-    ph[j] = layer_phase_ff(j == 0 ? wa : wb, j == 0 ? P.thickness_a : P.thickness_b, wl);
-  const LayerPhase A = ph[0], B = ph[1];
-  // one rolled loop over the polarisations keeps a single copy of the
-  // (large) float-float product code in the instruction cache
-  float R[2], T[2];
-#pragma unroll 1
-  for (int pol = 0; pol < 2; ++pol) {
-    cff q0, qa, qb, qs;
-    if (pol == 0) {
-      q0 = cff_scale(n0c, ff_of(cos0));
-      qa = wa;
-      qb = wb;
-      qs = ws;
-    } else {
-      q0 = cff_scale(cff_conj(n0c), ff_div(ff_of(cos0), cff_abs2(n0c)));
-      qa = p_factor(wa, na);
-      qb = p_factor(wb, nb);
-      qs = p_factor(ws, ns);
-    }
-    bilayer_pol_ff(q0, qa, qb, qs, A, B, P.num_periods, R[pol], T[pol]);
-  }
-  Rs = R[0];
-  Ts = T[0];
-  Rp = R[1];
-  Tp = T[1];
-}
-
 // R and T of one polarisation of a periodic bilayer mirror, two lanes per
 // sample: the even lane of a lane pair takes s, the odd lane p.  The even
 // lane evaluates layer A's medium factor and phase, the odd lane layer B's,
 // and the pair exchanges them by shuffles (both lanes of a pair always run
-// together); each lane then forms its own polarisation's product.  Half the
-// state of periodic_bilayer_ff per thread, twice the threads.
+// together); each lane then forms its own polarisation's product: half the
+// state of one thread evaluating both polarisations, twice the threads.
 __device__ __forceinline__ void periodic_bilayer_lane_ff(const otx_periodic_stack& P, float wl,
                                                          float cos0, cf n0, float& R, float& T) {
   const int lane = threadIdx.x & 31;
