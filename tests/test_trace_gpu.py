@@ -504,3 +504,32 @@ def test_attenuation_into_multilayer_mirror(cuda):
     # the multilayer tolerance of the single-precision transfer-matrix product
     assert np.abs(out["intensity"] - ref["intensity"]).max() < 1e-5
     assert np.allclose(out["attenuation"], ref["attenuation"], rtol=0, atol=0)
+
+
+def test_calls_beyond_the_launch_grid_stride(cuda):
+    """A call with more rays than the launch grid holds (4096 CTAs of 256
+    threads per SM) strides over them: it equals the same rays traced in
+    two calls of half the size, bit for bit, sensor image included."""
+    dev = torch.device("cuda", torch.cuda.current_device())
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    n = sms * 4096 * 256 + 12345
+    gen = torch.Generator(device=dev).manual_seed(17)
+    u = lambda lo, hi: lo + (hi - lo) * torch.rand(n, device=dev, generator=gen)  # noqa: E731
+    f = configs.FIELD_HALF
+    r, t = torch.sqrt(u(12.0**2, 50.0**2)), u(0.0, 2 * math.pi)  # the pupil annulus
+    g = dict(wavelength=u(400.0, 700.0), field_x=u(-f, f), field_y=u(-f, f),
+             pupil_x=r * torch.cos(t), pupil_y=r * torch.sin(t))
+    system = configs.newtonian(coated=True)
+    outs = ("px", "py", "unvignetted")
+    whole = run_rayfunction(system, g, image=True, outputs=outs)
+    h = n // 2
+    parts = [run_rayfunction(system, {k: v[a:b] for k, v in g.items()}, image=True, outputs=outs)
+             for a, b in ((0, h), (h, n))]
+    wo = whole.outputs
+    for k in ("x", "y"):
+        got = getattr(wo.position, k)
+        ref = torch.cat([getattr(p.outputs.position, k) for p in parts])
+        assert torch.equal(got, ref), k
+    assert torch.equal(wo.unvignetted, torch.cat([p.outputs.unvignetted for p in parts]))
+    assert int(wo.unvignetted.sum()) > 0.5 * n
+    assert torch.equal(whole.image[0], parts[0].image[0] + parts[1].image[0])
