@@ -239,14 +239,18 @@ __device__ __forceinline__ void bin_ray_warp(const otx_sensor& S, const otx_imag
   }
 }
 
-// Minimum resident CTAs per SM requested from the register allocator
-// (256 threads each).
-#ifndef OTX_TRACE_MIN_BLOCKS
-#define OTX_TRACE_MIN_BLOCKS 1
-#endif
+// Minimum resident CTAs per SM requested from the register allocator (256
+// threads each): 4 for the one-ray kernels without the layered multilayer
+// evaluator (64 registers, no spills: 3.41 ms per 5e7 rays of the precision
+// workload against 3.96 ms at their natural 79 registers and 3 CTAs, 3.65 ms
+// at 5 CTAs with spills); the others at their natural register counts.
+template <int RPT, bool ML>
+constexpr int trace_min_blocks() {
+  return (RPT == 1 && !ML) ? 4 : 1;
+}
 
 template <int RPT, int MODE, bool ACC, bool ML>
-__global__ void __launch_bounds__(256, OTX_TRACE_MIN_BLOCKS)
+__global__ void __launch_bounds__(256, trace_min_blocks<RPT, ML>())
     k_trace(const __grid_constant__ otx_system sys,
             const __grid_constant__ TraceArgs a) {
   const int64_t n = a.count;
