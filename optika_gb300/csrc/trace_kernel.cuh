@@ -243,10 +243,13 @@ __device__ __forceinline__ void bin_ray_warp(const otx_sensor& S, const otx_imag
 // threads each): 4 for the one-ray kernels without the layered multilayer
 // evaluator (64 registers, no spills: 3.41 ms per 5e7 rays of the precision
 // workload against 3.96 ms at their natural 79 registers and 3 CTAs, 3.65 ms
-// at 5 CTAs with spills); the others at their natural register counts.
+// at 5 CTAs with spills); 2 for the one-ray kernels with it (128 registers,
+// a few spilled bytes: 1.56 ms against 2.20 ms per 4e6 rays onto a 40-bilayer
+// mirror at their natural ~160 registers and 1 CTA); the two-ray kernels at
+// their natural register counts.
 template <int RPT, bool ML>
 constexpr int trace_min_blocks() {
-  return (RPT == 1 && !ML) ? 4 : 1;
+  return RPT != 1 ? 1 : (ML ? 2 : 4);
 }
 
 template <int RPT, int MODE, bool ACC, bool ML>
