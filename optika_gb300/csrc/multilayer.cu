@@ -21,23 +21,25 @@ struct MLArgs {
   float *rs, *rp, *ts, *tp;
 };
 
+// Two threads per sample: s on the even lane of a lane pair, p on the odd
+// one (the general evaluator shares nothing between the polarisations).
 __global__ void __launch_bounds__(128)
     k_multilayer(const __grid_constant__ otx_system sys, const __grid_constant__ MLArgs a) {
-  const int64_t step = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.count; i += step) {
+  const int64_t step = (int64_t)gridDim.x * blockDim.x / 2;
+  const bool odd = threadIdx.x & 1;
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 1; i < a.count; i += step) {
     const float wl = a.wl[i * a.s_wl];
     const float c0 = a.cosv[i * a.s_cos];
     const cf n0{a.n_re ? a.n_re[i * a.s_n] : 1.f, a.n_im ? a.n_im[i * a.s_n] : 0.f};
     int k = a.stack ? a.stack[i] : 0;
     k = (k < 0 || k >= OTX_MAX_STACKS) ? 0 : k;
     const SysStackSource src{sys, sys.stacks[k]};
-    float Rs, Rp, Ts, Tp;
-    multilayer_pol_ff<true>(src, wl, c0, n0, false, Rs, Ts);
-    multilayer_pol_ff<true>(src, wl, c0, n0, true, Rp, Tp);
-    if (a.rs) a.rs[i] = Rs;
-    if (a.rp) a.rp[i] = Rp;
-    if (a.ts) a.ts[i] = Ts;
-    if (a.tp) a.tp[i] = Tp;
+    float R, T;
+    multilayer_pol_ff<true>(src, wl, c0, n0, odd, R, T);
+    float* ro = odd ? a.rp : a.rs;
+    float* to = odd ? a.tp : a.ts;
+    if (ro) ro[i] = R;
+    if (to) to[i] = T;
   }
 }
 
@@ -125,7 +127,7 @@ extern "C" otx_status otx_multilayer_efficiency(
   }
   MLArgs a{count, wavelength, stride_wavelength, cos_incidence, stride_cos, n_re, n_im,
            stride_n, stack_index, r_s, r_p, t_s, t_p};
-  k_multilayer<<<ml_grid(count, 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*sys, a);
+  k_multilayer<<<ml_grid(2 * count, 128), 128, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*sys, a);
   return cudaGetLastError() == cudaSuccess ? OTX_OK : OTX_ERR_CUDA;
 }
 
