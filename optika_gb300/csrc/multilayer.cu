@@ -59,9 +59,10 @@ struct PeriodicArgs {
 // Two threads per sample (a lane pair: s on the even lane, p on the odd
 // one, sharing the two layer phases by shuffles); the sample's mirror is
 // read from the config table (L1/L2 resident: 40 B per config).  Four CTAs
-// per SM (128 registers): measured 5.00 ms per 1e7 samples against 5.06 at
-// three (167 registers), 5.10 at five (96, spilling) and 5.22 for one
-// thread per sample.
+// per SM (128 registers): measured 4.52 ms per 1e7 samples against 4.86 at
+// three (167 registers) and 4.53 at five (96, spilling); one thread per
+// sample took 5.22 ms (grid capped at 32 CTAs per SM, where lane pairs took
+// 5.00).
 __global__ void __launch_bounds__(128, 4)
     k_multilayer_periodic(const __grid_constant__ PeriodicArgs a) {
   const int64_t step = (int64_t)gridDim.x * blockDim.x / 2;
