@@ -66,3 +66,22 @@ def test_roofline_helpers_give_fractions_below_one():
     assert b._ncu_traffic("multilayer_periodic_1e7", 10) == pytest.approx(
         10 * _load("multilayer_periodic_1e7.json")["dram_bytes_per_unit"])
     assert b.issue_roofline("no_such_profile", 1, 1.0, pk, None) is None
+
+
+def test_reference_arm_line(tmp_path):
+    """`bench.py --impl reference` (the oracle on the host cores) prints one
+    JSON line with the fields the comparison reads, on a small sample."""
+    import subprocess
+    import sys
+
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps",
+                        "1", "--warmup", "0", "--ref-rays", "4000"],
+                       capture_output=True, text=True, cwd=tmp_path, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert line["unit"] == "rays*surfaces/s" and line["higher_is_better"] is True
+    assert line["value"] > 0 and line["cpu_baseline"]["value"] == line["value"]
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"],
+                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
