@@ -169,3 +169,35 @@ def test_two_rank_image_reduction_equals_single_process():
     c1, f1 = O.collect(s.sensor, r)
     assert np.array_equal(c, c1)
     assert np.allclose(f, f1)
+
+
+def test_affine_flags_select_the_device_frame_change():
+    """The lowering flags the frames the device changes by a cheaper form:
+    the identity rotation (plus the identity map when the translation is 0)
+    and rotations about y, which mix x and z only; any other rotation takes
+    the full 3 x 3 form.  Values are split exactly into hi + lo pairs."""
+    from optika_gb300 import _lib as L
+    from optika_gb300._lower import set_affine
+
+    def flags(m):
+        a = L.Affine()
+        set_affine(a, m)
+        return a.flags, a
+
+    m = np.eye(4)
+    assert flags(m)[0] == L.AFFINE_ROT_IDENTITY | L.AFFINE_IDENTITY
+    m[:3, 3] = [0.0, 0.0, 123.456]
+    f, a = flags(m)
+    assert f == L.AFFINE_ROT_IDENTITY
+    assert float(np.float32(a.t_hi[2])) + float(a.t_lo[2]) == pytest.approx(123.456, abs=1e-12)
+    c, s = np.cos(0.3), np.sin(0.3)
+    ry = np.eye(4)
+    ry[0, 0], ry[0, 2], ry[2, 0], ry[2, 2] = c, s, -s, c
+    assert flags(ry)[0] == L.AFFINE_ROT_Y
+    rx = np.eye(4)
+    rx[1, 1], rx[1, 2], rx[2, 1], rx[2, 2] = c, -s, s, c
+    assert flags(rx)[0] == 0
+    # the hi + lo split of every entry reproduces the float64 value to ~2^-48
+    f, a = flags(ry)
+    for i in range(9):
+        assert abs(float(a.m[i]) + float(a.m_lo[i]) - ry[:3, :3].flat[i]) < 1e-14
